@@ -1,0 +1,118 @@
+// Shared device helpers for the mcgb CUDA library (sm_103a).
+//
+// - Status codes and the thread-local error message behind mcgb_last_error().
+// - The per-site xoroshiro128+ stream (state = one 16-byte ulonglong2 {s0, s1},
+//   the layout of numba.cuda.random's xoroshiro128p_dtype) with the
+//   float32/float64 uniform conversions that the reference's kernels draw.
+// - complex64 helpers with the operation order the reference's complex64
+//   algebra uses (models/he3/update.py).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mcgb.h"
+
+namespace mcgb {
+
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t err, const char *what);
+int check_launch(const char *what);
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define MCGB_REQUIRE(cond, ...)                       \
+    do {                                              \
+        if (!(cond)) {                                \
+            ::mcgb::set_error(__VA_ARGS__);           \
+            return MCGB_EINVAL;                       \
+        }                                             \
+    } while (0)
+
+// ---------------------------------------------------------------- RNG
+
+__device__ __forceinline__ uint64_t rotl64(uint64_t x, int k)
+{
+    return (x << k) | (x >> (64 - k));
+}
+
+// One xoroshiro128+ step (a=55, b=14, c=36); returns s0 + s1 of the old state.
+__device__ __forceinline__ uint64_t xoro_next(ulonglong2 &s)
+{
+    uint64_t s0 = s.x, s1 = s.y;
+    uint64_t result = s0 + s1;
+    s1 ^= s0;
+    s.x = rotl64(s0, 55) ^ s1 ^ (s1 << 14);
+    s.y = rotl64(s1, 36);
+    return result;
+}
+
+// (x >> 11) * 2^-53 in float64.
+__device__ __forceinline__ double xoro_uniform_f64(ulonglong2 &s)
+{
+    return (double)(xoro_next(s) >> 11) * 0x1.0p-53;
+}
+
+// float32 of the float64 uniform.  The 53-bit integer m = x >> 11 converts to
+// float32 with one round-to-nearest-even step, and the power-of-two scale is
+// exact, so RN32(m) * 2^-53 equals float32(m * 2^-53) bit for bit, without
+// a float64 operation.
+__device__ __forceinline__ float xoro_uniform_f32(ulonglong2 &s)
+{
+    return __ull2float_rn(xoro_next(s) >> 11) * 0x1.0p-53f;
+}
+
+// ---------------------------------------------------------------- complex64
+
+struct c32 {
+    float re, im;
+};
+
+__device__ __forceinline__ c32 cmk(float a, float b) { return c32{a, b}; }
+__device__ __forceinline__ c32 operator+(c32 a, c32 b) { return cmk(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ c32 operator-(c32 a, c32 b) { return cmk(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ c32 operator-(c32 a) { return cmk(-a.re, -a.im); }
+__device__ __forceinline__ c32 operator*(c32 a, c32 b)
+{
+    return cmk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__device__ __forceinline__ c32 operator*(float s, c32 a) { return cmk(s * a.re, s * a.im); }
+__device__ __forceinline__ c32 conj(c32 a) { return cmk(a.re, -a.im); }
+__device__ __forceinline__ float norm2(c32 z) { return z.re * z.re + z.im * z.im; }
+
+// ---------------------------------------------------------------- reductions
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NC channels (blockDim.x a multiple of 32, <= 1024).
+// Result valid in thread 0.  `scratch` holds 32*NC doubles.
+template <int NC>
+__device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) v[c] = warp_sum(v[c]);
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) scratch[c * 32 + warp] = v[c];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            double x = lane < nwarps ? scratch[c * 32 + lane] : 0.0;
+            v[c] = warp_sum(x);
+        }
+    }
+}
+
+__host__ __device__ __forceinline__ int wrapi(int i, int L) { return i < 0 ? i + L : (i >= L ? i - L : i); }
+
+}  // namespace mcgb
