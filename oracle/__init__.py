@@ -60,6 +60,7 @@ def _declare(L):
         "orc_splitmix64_first": (_U64, [_U64]),
         "orc_ising_update_color": (None, [_P, _P, _P, _I, _I, _I, _F]),
         "orc_ising_sweeps": (None, [_P, _P, _P, _I, _I, _F, _I, _I]),
+        "orc_ising_sweeps_tab": (None, [_P, _P, _P, _P, _I, _I, _F, _I, _I]),
         "orc_ising_energy": (None, [_P, _I, _I, _F, _P]),
         "orc_ising_measure": (None, [_P, _I, _I, _F, _P, _P, _P]),
         "orc_xy_update_color": (None, [_P, _P, _P, _I, _I, _I, _F, _F]),
@@ -150,6 +151,23 @@ def ising_sweeps(spins, rng, betas, J, n_sweeps, n_threads=1):
     R, L = spins.shape[0], spins.shape[1]
     lib().orc_ising_sweeps(_ptr(_check(spins, np.int8, "spins")), _ptr(_check(rng, np.uint64, "rng")),
                            _ptr(_check(betas, np.float32, "betas")), R, L, J, n_sweeps, n_threads)
+
+
+def ising_exponent_arguments(betas, J):
+    """float32 arguments -beta * (float32(k) * J), k = -8, -4, 0, 4, 8, shape (R, 5)."""
+    k = np.array([-8, -4, 0, 4, 8], dtype=np.float32)
+    return (-np.asarray(betas, np.float32)[:, None] * (k[None, :] * np.float32(J))).astype(np.float32)
+
+
+def ising_sweeps_tab(spins, rng, betas, table, J, n_sweeps, n_threads=1):
+    """Sweeps whose acceptance exponentials come from ``table`` (R, 5) float32."""
+    R, L = spins.shape[0], spins.shape[1]
+    tab = np.ascontiguousarray(table, dtype=np.float32)
+    if tab.shape != (R, 5):
+        raise ValueError("table must have shape (R, 5)")
+    lib().orc_ising_sweeps_tab(_ptr(_check(spins, np.int8, "spins")), _ptr(_check(rng, np.uint64, "rng")),
+                               _ptr(_check(betas, np.float32, "betas")), _ptr(tab), R, L, J, n_sweeps,
+                               n_threads)
 
 
 def ising_energy(spins, J):

@@ -106,8 +106,13 @@ static inline int wrap(int i, int L) { return (i % L + L) % L; }
 /* Ising: models/ising/update.py:7-29, models/ising/measure.py:10-99        */
 /* ------------------------------------------------------------------------ */
 
-static void ising_color_replica(int8_t *spins, uint64_t *rng, float beta, int r, int L,
-                                int color, float J)
+/* `tab` (5 floats, may be NULL) supplies exp(-beta*dE) for the five
+ * possible dE = float32(k) * J, k = -8, -4, 0, 4, 8 (index (k + 8) / 4).  The
+ * reference evaluates this with CUDA's float32 expf (libdevice), which is not
+ * always correctly rounded; a test can pass the values a GPU's expf produced
+ * so that the lattices stay bit-exact.  NULL evaluates libm expf. */
+static void ising_color_replica(int8_t *spins, uint64_t *rng, float beta, const float *tab, int r,
+                                int L, int color, float J)
 {
     const int8_t *base = spins + (int64_t)r * L * L;
     for (int i = color / 2; i < L; i += 2)
@@ -118,10 +123,11 @@ static void ising_color_replica(int8_t *spins, uint64_t *rng, float beta, int r,
             int left = base[i * L + wrap(j - 1, L)];
             int right = base[i * L + wrap(j + 1, L)];
             /* float32(2*s*sum) * J, then a float32 exp of -beta*dE. */
-            float dE = (float)(2 * s * (up + down + left + right)) * J;
+            int k = 2 * s * (up + down + left + right);
+            float dE = (float)k * J;
             int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
             float u = orc_rng_uniform_f32(rng + 2 * idx);
-            if (dE <= 0.0f || u < expf(-beta * dE))
+            if (dE <= 0.0f || u < (tab ? tab[(k + 8) / 4] : expf(-beta * dE)))
                 spins[(int64_t)r * L * L + i * L + j] = (int8_t)(-s);
         }
 }
@@ -129,17 +135,24 @@ static void ising_color_replica(int8_t *spins, uint64_t *rng, float beta, int r,
 void orc_ising_update_color(int8_t *spins, uint64_t *rng, const float *betas, int R, int L,
                             int color, float J)
 {
-    for (int r = 0; r < R; ++r) ising_color_replica(spins, rng, betas[r], r, L, color, J);
+    for (int r = 0; r < R; ++r) ising_color_replica(spins, rng, betas[r], NULL, r, L, color, J);
 }
 
 void orc_ising_sweeps(int8_t *spins, uint64_t *rng, const float *betas, int R, int L,
                       float J, int n_sweeps, int n_threads)
 {
+    orc_ising_sweeps_tab(spins, rng, betas, NULL, R, L, J, n_sweeps, n_threads);
+}
+
+void orc_ising_sweeps_tab(int8_t *spins, uint64_t *rng, const float *betas, const float *tab,
+                          int R, int L, float J, int n_sweeps, int n_threads)
+{
     (void)n_threads;
     OMP_FOR_R
     for (int r = 0; r < R; ++r)
         for (int s = 0; s < n_sweeps; ++s)
-            for (int c = 0; c < 4; ++c) ising_color_replica(spins, rng, betas[r], r, L, c, J);
+            for (int c = 0; c < 4; ++c)
+                ising_color_replica(spins, rng, betas[r], tab ? tab + 5 * r : NULL, r, L, c, J);
 }
 
 void orc_ising_energy(const int8_t *spins, int R, int L, float J, double *out)

@@ -39,6 +39,10 @@ void orc_ising_update_color(int8_t *spins, uint64_t *rng, const float *betas,
                             int R, int L, int color, float J);
 void orc_ising_sweeps(int8_t *spins, uint64_t *rng, const float *betas,
                       int R, int L, float J, int n_sweeps, int n_threads);
+/* As orc_ising_sweeps with a per-replica table (R x 5) of the acceptance
+ * exponentials exp(-beta * float32(k) * J), k = -8, -4, 0, 4, 8. */
+void orc_ising_sweeps_tab(int8_t *spins, uint64_t *rng, const float *betas, const float *tab,
+                          int R, int L, float J, int n_sweeps, int n_threads);
 void orc_ising_energy(const int8_t *spins, int R, int L, float J, double *out);
 void orc_ising_measure(const int8_t *spins, int R, int L, float J,
                        const int32_t *temperature_indices, const double *cached,

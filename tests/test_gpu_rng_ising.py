@@ -55,22 +55,27 @@ def _ising_runtime(L, temperatures, seed, init_seed):
     return rt, spins
 
 
-def test_cuda_expf_equals_correctly_rounded_exp_on_ising_thresholds(dev):
-    """The only exponentials an Ising update evaluates are expf(-beta*4J) and
-    expf(-beta*8J); bit-exact lattices need CUDA's expf to agree with the
-    oracle's libm expf there."""
-    device, _ = dev
-    from mcgb import _lib
+def cuda_ising_table(betas, J):
+    """CUDA expf of the five Ising acceptance arguments per replica, (R, 5)."""
+    from mcgb import _lib, device
+    args = oracle.ising_exponent_arguments(betas, J)
+    x = device.to_device(args)
+    y = device.device_array(args.shape, np.float32)
+    _lib.call("mcgb_expf", x.cptr, y.cptr, args.size, _lib.stream_handle())
+    return y.copy_to_host()
+
+
+def test_cuda_expf_within_documented_error_of_exact_exp(dev):
+    """The reference's acceptance exponential is CUDA's float32 expf (its
+    documented bound is 2 ulp).  Check that bound on the Ising arguments; the
+    oracle then takes these CUDA values as inputs (orc_ising_sweeps_tab)."""
     betas = (1.0 / np.array([1.5, 2.269, 3.0, 2.0, 2.5, 0.6, 0.8, 1.0])).astype(np.float32)
-    xs = np.concatenate([-betas * np.float32(4.0), -betas * np.float32(8.0),
-                         -betas * (np.float32(4.0) * np.float32(1.37)),
-                         -betas * (np.float32(8.0) * np.float32(1.37))]).astype(np.float32)
-    x = device.to_device(xs)
-    y = device.device_array(xs.shape, np.float32)
-    _lib.call("mcgb_expf", x.cptr, y.cptr, len(xs), _lib.stream_handle())
-    cuda = y.copy_to_host()
-    libm = np.array([np.float32(np.exp(np.float64(v))) for v in xs], np.float32)
-    np.testing.assert_array_equal(cuda, libm)
+    for J in (1.0, 1.37, 0.9):
+        cuda = cuda_ising_table(betas, J)
+        args = oracle.ising_exponent_arguments(betas, J)
+        exact = np.exp(args.astype(np.float64))
+        ulp = np.spacing(exact.astype(np.float32)).astype(np.float64)
+        assert np.all(np.abs(cuda - exact) <= 2 * ulp)
 
 
 @pytest.mark.parametrize("T", [1.5, 2.269, 3.0])
@@ -83,7 +88,8 @@ def test_ising_lattice_bit_exact_after_100_sweeps(T):
     got = rt.snapshot()
     ref = spins.copy()
     ref_rng = oracle.rng_states(L * L, 42 + L)
-    oracle.ising_sweeps(ref, ref_rng, np.array([1 / T], np.float32), np.float32(1), 100)
+    betas = np.array([1 / T], np.float32)
+    oracle.ising_sweeps_tab(ref, ref_rng, betas, cuda_ising_table(betas, 1.0), np.float32(1), 100)
     np.testing.assert_array_equal(got, ref)
     rs = rt.rng_states.copy_to_host()
     np.testing.assert_array_equal(rs["s0"], ref_rng[:, 0])
