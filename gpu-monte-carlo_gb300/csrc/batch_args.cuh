@@ -1,0 +1,154 @@
+// Kernel-side argument block of the batched engine and the host helpers that
+// validate a mcgb_batch_window and launch a window kernel with its cluster
+// shape.
+#pragma once
+
+#include "batch_window.cuh"
+
+namespace mcgb {
+
+struct BatchArgs {
+    WindowCommon c;
+    void *state;
+    float2 *aux;
+    float J, delta;
+    const float *sigma_t;
+    float coeff[5];
+    float K, g_d, rho, mass;
+    long long *counters;
+    int n_replicas;
+};
+
+inline BatchArgs make_args(const mcgb_batch_window &w)
+{
+    BatchArgs a;
+    a.c.table = w.table;
+    a.c.work_ptr = w.work_ptr;
+    a.c.work_idx = w.work_idx;
+    a.c.rng = w.rng;
+    a.c.betas = w.betas;
+    a.c.w2t = w.w2t;
+    a.c.e_run = w.e_run;
+    a.c.energies = w.energies;
+    a.c.accepted = w.accepted;
+    a.c.samples = w.samples;
+    a.c.staging = w.staging;
+    a.c.n_temps_total = w.n_temps_total;
+    a.c.n_slots = w.n_slots;
+    a.c.clock = reinterpret_cast<const long long *>(w.clock);
+    a.c.first_sample_sweep = w.first_sample_sweep;
+    a.c.sample_interval = w.sample_interval;
+    a.c.n_sweeps = w.n_sweeps;
+    a.state = w.state;
+    a.aux = static_cast<float2 *>(w.aux);
+    a.J = w.J;
+    a.delta = w.delta;
+    a.sigma_t = w.sigma_t;
+    for (int q = 0; q < 5; ++q) a.coeff[q] = w.coefficients[q];
+    a.K = w.K;
+    a.g_d = w.g_d;
+    a.rho = w.rho;
+    a.mass = w.mass;
+    a.counters = w.counters;
+    a.n_replicas = w.n_replicas;
+    return a;
+}
+
+// Largest plaquette count a CTA holds, after validating the table against
+// the cluster shape.  Returns a negative status on error.
+inline long long validate_window(const mcgb_batch_window &w)
+{
+    MCGB_REQUIRE(w.table && w.host_table && w.work_ptr && w.work_idx, "batch window: null table/work list");
+    MCGB_REQUIRE(w.state && w.rng && w.betas && w.w2t && w.e_run && w.energies && w.accepted && w.clock,
+                 "batch window: null state pointer");
+    MCGB_REQUIRE(w.n_replicas >= 1 && w.n_clusters >= 1, "batch window: empty batch");
+    MCGB_REQUIRE(w.cluster_size >= 1 && w.cluster_size <= 16, "batch window: cluster_size must be 1..16");
+    MCGB_REQUIRE(w.threads >= 32 && w.threads <= 1024 && w.threads % 32 == 0,
+                 "batch window: threads must be a multiple of 32 in [32, 1024]");
+    MCGB_REQUIRE(w.n_sweeps >= 0, "batch window: n_sweeps must be >= 0");
+    MCGB_REQUIRE(w.samples == nullptr || (w.n_slots >= 1 && w.n_temps_total >= 1 && w.sample_interval >= 1),
+                 "batch window: bad sample buffer");
+    long long max_npl = 0;
+    for (int r = 0; r < w.n_replicas; ++r) {
+        const mcgb_replica &rep = w.host_table[r];
+        MCGB_REQUIRE(rep.L >= 4 && rep.L % (2 * w.cluster_size) == 0,
+                     "batch window: replica %d has L=%d, not a multiple of 2*cluster_size=%d", r, rep.L,
+                     2 * w.cluster_size);
+        MCGB_REQUIRE(rep.ladder_start >= 0 && rep.ladder_start + rep.n_temps <= w.n_replicas &&
+                         rep.ladder_start <= r && r < rep.ladder_start + rep.n_temps,
+                     "batch window: replica %d has an inconsistent ladder range", r);
+        MCGB_REQUIRE(rep.state_offset >= 0, "batch window: negative state offset");
+        const long long npl = (long long)rep.L * rep.L / (4 * w.cluster_size);
+        if (npl > max_npl) max_npl = npl;
+    }
+    MCGB_REQUIRE(w.samples == nullptr || w.n_temps_total >= w.n_replicas,
+                 "batch window: n_temps_total must cover every replica");
+    return max_npl;
+}
+
+template <class M, int NPMAX>
+int launch_window(const BatchArgs &a, const mcgb_batch_window &w, long long max_npl, cudaStream_t stream,
+                  const char *name)
+{
+    auto kern = window_kernel<M, NPMAX>;
+    const size_t smem = window_smem_bytes<M>((int)max_npl);
+    MCGB_REQUIRE(smem <= 232448, "%s: a strip needs %zu bytes of shared memory (> 227 KB); use a larger "
+                                 "cluster_size", name, smem);
+    int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "cudaFuncSetAttribute(max dynamic smem)");
+    if (st) return st;
+    if (w.cluster_size > 8) {
+        st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                         "cudaFuncSetAttribute(non-portable cluster)");
+        if (st) return st;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(w.n_clusters * w.cluster_size));
+    cfg.blockDim = dim3((unsigned)w.threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)w.cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cuda_status(cudaLaunchKernelEx(&cfg, kern, a), name);
+}
+
+template <class M, int NPMAX>
+int max_clusters_for(int C, int threads, size_t smem, int *out)
+{
+    auto kern = window_kernel<M, NPMAX>;
+    int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "cudaFuncSetAttribute(max dynamic smem)");
+    if (st) return st;
+    if (C > 8) {
+        st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                         "cudaFuncSetAttribute(non-portable cluster)");
+        if (st) return st;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(C * 256));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cuda_status(cudaOccupancyMaxActiveClusters(out, kern, &cfg), "cudaOccupancyMaxActiveClusters");
+}
+
+// Colour-major plane index of site (i, j) of a replica of size L.
+__host__ __device__ __forceinline__ int64_t cm_index(int i, int j, int L)
+{
+    const int LP = L >> 1;
+    const int c = ((i & 1) << 1) | (j & 1);
+    return (int64_t)c * LP * LP + (int64_t)(i >> 1) * LP + (j >> 1);
+}
+
+}  // namespace mcgb

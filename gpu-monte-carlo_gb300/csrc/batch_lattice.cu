@@ -1,0 +1,288 @@
+// Batched-engine policies for the Ising and XY models (mixed precision).
+//
+// Ising (models/ising/update.py:7-29): int8 spins in shared memory, one RNG
+// draw per visit, acceptance `dE <= 0 or u < expf(-beta*dE)` with the five
+// possible expf values per replica evaluated once per window with the same
+// float32 expf -- bit-identical to the per-colour kernel.  The window's final
+// energy is the exact integer bond count times J.
+//
+// XY (models/xy/update.py:6-54 and the Gaussian variant): shared memory
+// holds (cos, sin) of every angle, so an update evaluates one sincos of the
+// proposal instead of eight cosines:
+//   dE = -J [ (cos t' - cos t) S_c + (sin t' - sin t) S_s ],
+// S_c, S_s the sums over the four neighbours' cached (cos, sin).  Proposal,
+// Box-Muller and acceptance use the fast float32 intrinsics; the draw
+// sequence per visit is the oracle's (uniform: u, v; Gaussian: u1, u2, v).
+// Accepted changes accumulate per thread with compensation and update the
+// replica's running energy; samples read it instead of re-summing bonds.
+#include "batch_args.cuh"
+
+namespace mcgb {
+
+// ================================================================= Ising
+
+struct IsingPolicy {
+    using Args = BatchArgs;
+    using Cell = int8_t;
+    static constexpr int kOwnFloats = 0;
+    static constexpr int kChannels = 2;  // energy, magnetization
+    static constexpr bool kSplitMiddle = false;
+    static constexpr bool kEnergyFromDelta = false;
+    static constexpr bool kExactEnergy = true;
+
+    struct Ctx {
+        float t[5];  // acceptance thresholds for k = -8, -4, 0, 4, 8
+        float J;
+    };
+
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
+    {
+        Ctx x;
+        x.J = a.J;
+        const float beta = a.c.betas[r];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const float dE = (float)(4 * q - 8) * a.J;
+            // u <= 1 < 2 accepts every move with dE <= 0.
+            x.t[q] = dE <= 0.0f ? 2.0f : expf(-beta * dE);
+        }
+        return x;
+    }
+    static __device__ __forceinline__ void load(const Args &a, int64_t site, Cell &cell, float *)
+    {
+        cell = static_cast<const int8_t *>(a.state)[site];
+    }
+    static __device__ __forceinline__ void store(const Args &a, int64_t site, const Cell &cell, const float *)
+    {
+        static_cast<int8_t *>(a.state)[site] = cell;
+    }
+    template <int C_>
+    static __device__ __forceinline__ bool update(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *,
+                                                  ulonglong2 &st, float &dE)
+    {
+        const int s = me;
+        const int sum = nb.at(nbr_up(C_)) + nb.at(nbr_down(C_)) + nb.at(nbr_left(C_)) + nb.at(nbr_right(C_));
+        const int k = 2 * s * sum;
+        const float u = xoro_uniform_f32(st);
+        dE = (float)k * x.J;
+        // Static indices keep the five thresholds in registers.
+        float t = x.t[0];
+        t = k == -4 ? x.t[1] : t;
+        t = k == 0 ? x.t[2] : t;
+        t = k == 4 ? x.t[3] : t;
+        t = k == 8 ? x.t[4] : t;
+        if (u < t) {
+            me = (int8_t)(-s);
+            return true;
+        }
+        return false;
+    }
+    template <int C_>
+    static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
+                                                   const float *, double *v)
+    {
+        const int s = me;
+        v[0] += (double)(s * (nb.at(nbr_down(C_)) + nb.at(nbr_right(C_))));
+        v[1] += (double)s;
+    }
+    template <int C_>
+    static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
+                                                       const float *, double &e)
+    {
+        e += (double)(me * (nb.at(nbr_down(C_)) + nb.at(nbr_right(C_))));
+    }
+    static __device__ __forceinline__ void finish_sample(const Ctx &x, double *v) { v[0] *= -(double)x.J; }
+    static __device__ __forceinline__ double finish_energy(const Ctx &x, double bonds) { return -(double)x.J * bonds; }
+};
+
+// ================================================================= XY
+
+struct XYPolicy {
+    using Args = BatchArgs;
+    using Cell = float2;  // (cos theta, sin theta)
+    static constexpr int kOwnFloats = 1;  // theta
+    static constexpr int kChannels = 5;   // energy, mx, my, twist_cos_x, twist_sin_x
+    static constexpr bool kSplitMiddle = false;
+    static constexpr bool kEnergyFromDelta = true;
+    static constexpr bool kExactEnergy = false;
+
+    struct Ctx {
+        float beta, sigma, J, delta;
+        bool gauss;
+    };
+
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
+    {
+        Ctx x;
+        x.beta = a.c.betas[r];
+        x.J = a.J;
+        x.delta = a.delta;
+        x.gauss = a.sigma_t != nullptr;
+        x.sigma = x.gauss ? a.sigma_t[rep.ladder_start + a.c.w2t[r]] : 0.0f;
+        return x;
+    }
+    // The (cos, sin) cache persists in `aux` between windows, so the chain
+    // always evaluates the energy of the values its updates computed.
+    static __device__ __forceinline__ void load(const Args &a, int64_t site, Cell &cell, float *own)
+    {
+        own[0] = static_cast<const float *>(a.state)[site];
+        cell = a.aux[site];
+    }
+    static __device__ __forceinline__ void store(const Args &a, int64_t site, const Cell &cell, const float *own)
+    {
+        static_cast<float *>(a.state)[site] = own[0];
+        a.aux[site] = cell;
+    }
+    template <int C_>
+    static __device__ __forceinline__ bool update(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *own,
+                                                  ulonglong2 &st, float &dE)
+    {
+        const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
+        const float2 a = nb.at(nbr_up(C_)), b = nb.at(nbr_down(C_));
+        const float2 c = nb.at(nbr_left(C_)), d = nb.at(nbr_right(C_));
+        const float sc = (a.x + b.x) + (c.x + d.x);
+        const float ss = (a.y + b.y) + (c.y + d.y);
+        const float t = own[0];
+        float tp;
+        if (x.gauss) {
+            float u1 = xoro_uniform_f32(st);
+            const float u2 = xoro_uniform_f32(st);
+            if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
+            // cos(2 pi u2) = -cos(2 pi u2 - pi), evaluated on [-pi, pi].
+            const float z = -sqrtf(-2.0f * __logf(u1)) * __cosf(fmaf(two_pi, u2, -pi));
+            tp = fmaf(x.sigma, z, t);
+            tp -= two_pi * floorf((tp + pi) * (1.0f / two_pi));
+            if (tp >= pi) tp -= two_pi;
+            if (tp < -pi) tp += two_pi;
+        } else {
+            const float u = xoro_uniform_f32(st);
+            tp = t + x.delta * (2.0f * u - 1.0f);
+            if (tp >= pi) tp -= two_pi;
+            else if (tp < -pi) tp += two_pi;
+        }
+        float sp, cp;
+        __sincosf(tp, &sp, &cp);
+        dE = -x.J * ((cp - me.x) * sc + (sp - me.y) * ss);
+        const float v = xoro_uniform_f32(st);
+        if (dE <= 0.0f || v < __expf(-x.beta * dE)) {
+            own[0] = tp;
+            me = make_float2(cp, sp);
+            return true;
+        }
+        return false;
+    }
+    template <int C_>
+    static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
+                                                   const float *, double *v)
+    {
+        const float2 dn = nb.at(nbr_down(C_));
+        v[1] += me.x;
+        v[2] += me.y;
+        v[3] += me.x * dn.x + me.y * dn.y;
+        v[4] += me.y * dn.x - me.x * dn.y;
+    }
+    template <int C_>
+    static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &, const Cell &,
+                                                       const float *, double &)
+    {
+    }
+    static __device__ __forceinline__ void finish_sample(const Ctx &, double *) {}
+    static __device__ __forceinline__ double finish_energy(const Ctx &, double e) { return e; }
+};
+
+// ================================================================= FP64 energies
+
+// Site (i, j) of a colour-major replica.
+template <typename T>
+__device__ __forceinline__ const T &cm_at(const T *base, int i, int j, int L)
+{
+    return base[cm_index(i, j, L)];
+}
+
+// Exact total energy of each replica (one block per replica), float64.
+// model: 0 Ising (integer bond count times J), 1 XY (float64 cos).
+__global__ void batch_energy64_kernel(int model, const void *state, const mcgb_replica *table, float J,
+                                      float *e_run, double *energies, double *drift)
+{
+    __shared__ double scratch[32];
+    const int r = blockIdx.x;
+    const mcgb_replica rep = table[r];
+    const int L = rep.L;
+    double v[1] = {0.0};
+    for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
+        const int i = k / L, j = k - i * L;
+        const int id = i + 1 == L ? 0 : i + 1, jr = j + 1 == L ? 0 : j + 1;
+        if (model == MCGB_MODEL_ISING) {
+            const int8_t *b = static_cast<const int8_t *>(state) + rep.state_offset;
+            v[0] += (double)(cm_at(b, i, j, L) * (cm_at(b, id, j, L) + cm_at(b, i, jr, L)));
+        } else {
+            const float *b = static_cast<const float *>(state) + rep.state_offset;
+            const double t = cm_at(b, i, j, L);
+            v[0] += -(double)J * (cos(t - (double)cm_at(b, id, j, L)) + cos(t - (double)cm_at(b, i, jr, L)));
+        }
+    }
+    block_sum<1>(v, scratch);
+    if (threadIdx.x == 0) {
+        const double e = model == MCGB_MODEL_ISING ? -(double)J * v[0] : v[0];
+        if (drift) drift[r] = ((double)e_run[2 * r] + (double)e_run[2 * r + 1]) - e;
+        const float hi = (float)e;
+        e_run[2 * r] = hi;
+        e_run[2 * r + 1] = (float)(e - (double)hi);
+        energies[r] = e;
+    }
+}
+
+__global__ void refresh_aux_kernel(const float *state, float2 *aux, int64_t n, int stride)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float sn, cs;
+    sincosf(state[k * stride], &sn, &cs);
+    aux[k] = make_float2(cs, sn);
+}
+
+int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s)
+{
+    MCGB_REQUIRE(w.aux && w.state && w.host_table && w.n_replicas >= 1, "refresh_aux: null pointer");
+    const mcgb_replica &last = w.host_table[w.n_replicas - 1];
+    const int64_t n = last.state_offset + (int64_t)last.L * last.L;
+    refresh_aux_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const float *>(w.state),
+                                                                    static_cast<float2 *>(w.aux), n, stride);
+    return check_launch("refresh_aux_kernel");
+}
+
+int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s)
+{
+    if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w.aux != nullptr, "XY window: null (cos, sin) cache");
+    const long long max_npl = validate_window(w);
+    if (max_npl < 0) return (int)max_npl;
+    const BatchArgs a = make_args(w);
+    if (model == MCGB_MODEL_ISING)
+        return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, max_npl, s, "ising window")
+                               : launch_window<IsingPolicy, 2>(a, w, max_npl, s, "ising window");
+    return w.threads > 512 ? launch_window<XYPolicy, 1>(a, w, max_npl, s, "xy window")
+                           : launch_window<XYPolicy, 2>(a, w, max_npl, s, "xy window");
+}
+
+int lattice_smem(int model, long long max_npl)
+{
+    return (int)(model == MCGB_MODEL_ISING ? window_smem_bytes<IsingPolicy>((int)max_npl)
+                                           : window_smem_bytes<XYPolicy>((int)max_npl));
+}
+
+int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out)
+{
+    if (model == MCGB_MODEL_ISING)
+        return threads > 512 ? max_clusters_for<IsingPolicy, 1>(C, threads, smem, out)
+                             : max_clusters_for<IsingPolicy, 2>(C, threads, smem, out);
+    return threads > 512 ? max_clusters_for<XYPolicy, 1>(C, threads, smem, out)
+                         : max_clusters_for<XYPolicy, 2>(C, threads, smem, out);
+}
+
+int lattice_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s)
+{
+    batch_energy64_kernel<<<w.n_replicas, 256, 0, s>>>(model, w.state, w.table, w.J, w.e_run, w.energies, drift);
+    return check_launch("batch_energy64_kernel");
+}
+
+}  // namespace mcgb

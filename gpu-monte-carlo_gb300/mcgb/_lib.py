@@ -46,6 +46,23 @@ SIGNATURES = {
     "mcgb_he3_local_differences": [_P, _I, _I, _P, _P, _I, _P, _F, _F, _P, _P],
     "mcgb_pt_exchange": [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I64, _P],
     "mcgb_pt_record_walkers": [_P, _P, _P, _I, _P],
+    "mcgb_batch_channels": [_I],
+    "mcgb_batch_smem_bytes": [_I, _I64],
+    "mcgb_batch_max_clusters": [_I, _I, _I, _I64, _P],
+    "mcgb_batch_window_run": [_I, _P, _P],
+    "mcgb_batch_permute": [_P, _P, _I64, _P, _P, _I, _I, _I, _P],
+    "mcgb_batch_refresh_aux": [_I, _P, _P],
+    "mcgb_batch_recompute_energy": [_I, _P, _P, _P],
+    "mcgb_batch_exchange": [_P, _P, _P],
+    "mcgb_batch_clock_tick": [_P, _I, _I, _P],
+    "mcgb_batch_tune_sigma": [_P, _P, _P, _P, _P, _I, _I, _F, _F, _F, _F, _P],
+}
+
+# Entry points whose return value is not an int status.
+RESTYPES = {
+    "mcgb_last_error": ctypes.c_char_p,
+    "mcgb_version": ctypes.c_char_p,
+    "mcgb_batch_smem_bytes": ctypes.c_int64,
 }
 
 EINVAL, ECUDA, ENOMEM, ETIMEOUT = -1, -2, -3, -4
@@ -86,7 +103,7 @@ def load():
             handle.mcgb_version.argtypes = []
             for name, args in SIGNATURES.items():
                 fn = getattr(handle, name)
-                fn.restype = ctypes.c_int
+                fn.restype = RESTYPES.get(name, ctypes.c_int)
                 fn.argtypes = args
             _lib = handle
     return _lib

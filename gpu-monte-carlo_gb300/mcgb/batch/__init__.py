@@ -1,0 +1,650 @@
+"""Batched ladder engine: every replica of every ladder in one launch per window.
+
+The reference runs one ``Runtime`` per (L, temperature ladder), four kernel
+launches per sweep, an energy reduction and an exchange kernel every
+``exchange_interval`` sweeps and a measurement kernel plus a host copy per
+sample (core/runtime.py:87-99, core/parallel_tempering.py:245-273,
+core/simulation.py:28-96).  :class:`LadderBatch` runs the same schedule for a
+table of replicas of any mix of L: one cluster-per-replica window kernel of
+``exchange_interval`` sweeps (state in shared memory, RNG in registers), one
+exchange kernel over all ladders and a clock tick, captured as a CUDA graph
+and replayed; samples accumulate in a device buffer that is copied once.
+
+Replica (L, ladder k, slot t) keeps the RNG stream that a ``Runtime`` of that
+ladder with seed ``seeds[k]`` gives the same site, so an Ising batch is
+bit-identical to the per-colour path; the exchange streams of ladder k equal
+``ParallelTempering``'s with ``exchange_seeds[k]``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import heapq
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..device import XOROSHIRO128P_DTYPE, DeviceArray, device_zeros, ptr, to_device
+from ..rng import create_xoroshiro128p_states
+
+REPLICA_DTYPE = np.dtype([("L", "<i4"), ("ladder", "<i4"), ("ladder_start", "<i4"),
+                          ("n_temps", "<i4"), ("state_offset", "<i8")])
+
+MODEL_ISING, MODEL_XY, MODEL_KAWAMURA, MODEL_HE3, MODEL_HE3_GAUSS = range(5)
+
+CHANNELS = {
+    MODEL_ISING: ("energy", "magnetization"),
+    MODEL_XY: ("energy", "mx", "my", "twist_cos_x", "twist_sin_x"),
+    MODEL_KAWAMURA: ("energy", "chirality", "px", "py", "spin2", "twist_cos_x", "twist_sin_x"),
+    MODEL_HE3: ("energy", "density", "chirality", "phase_real", "phase_imag",
+                "current_x", "curvature_x", "current_y", "curvature_y", "spin_alignment"),
+}
+CHANNELS[MODEL_HE3_GAUSS] = CHANNELS[MODEL_HE3]
+
+
+class BatchWindow(ctypes.Structure):
+    """ctypes mirror of ``mcgb_batch_window`` (include/mcgb.h)."""
+
+    _fields_ = [
+        ("table", ctypes.c_void_p), ("host_table", ctypes.c_void_p), ("n_replicas", ctypes.c_int32),
+        ("work_ptr", ctypes.c_void_p), ("work_idx", ctypes.c_void_p),
+        ("n_clusters", ctypes.c_int32), ("cluster_size", ctypes.c_int32), ("threads", ctypes.c_int32),
+        ("state", ctypes.c_void_p), ("rng", ctypes.c_void_p), ("aux", ctypes.c_void_p),
+        ("betas", ctypes.c_void_p),
+        ("w2t", ctypes.c_void_p), ("e_run", ctypes.c_void_p), ("energies", ctypes.c_void_p),
+        ("accepted", ctypes.c_void_p), ("counters", ctypes.c_void_p), ("samples", ctypes.c_void_p),
+        ("staging", ctypes.c_void_p),
+        ("n_temps_total", ctypes.c_int32), ("n_slots", ctypes.c_int32),
+        ("clock", ctypes.c_void_p), ("first_sample_sweep", ctypes.c_int64),
+        ("sample_interval", ctypes.c_int32), ("n_sweeps", ctypes.c_int32),
+        ("J", ctypes.c_float), ("delta", ctypes.c_float), ("sigma_t", ctypes.c_void_p),
+        ("coefficients", ctypes.c_float * 5), ("K", ctypes.c_float), ("g_d", ctypes.c_float),
+        ("rho", ctypes.c_float), ("mass", ctypes.c_float),
+    ]
+
+
+class BatchPT(ctypes.Structure):
+    """ctypes mirror of ``mcgb_batch_pt``."""
+
+    _fields_ = [
+        ("t2w", ctypes.c_void_p), ("rng", ctypes.c_void_p), ("swap_counts", ctypes.c_void_p),
+        ("trips", ctypes.c_void_p), ("ladder_starts", ctypes.c_void_p), ("ladder_sizes", ctypes.c_void_p),
+        ("n_ladders", ctypes.c_int32), ("channels", ctypes.c_int32),
+    ]
+
+
+def _model_info(model, gaussian):
+    from ..models.he3.model import He3Model
+    from ..models.ising.model import IsingModel
+    from ..models.kawamura.model import KawamuraModel
+    from ..models.xy.model import XYModel
+
+    if isinstance(model, IsingModel):
+        return MODEL_ISING, np.dtype(np.int8), ()
+    if isinstance(model, XYModel):
+        return MODEL_XY, np.dtype(np.float32), ()
+    if isinstance(model, KawamuraModel):
+        return MODEL_KAWAMURA, np.dtype(np.float32), (5,)
+    if isinstance(model, He3Model):
+        return (MODEL_HE3_GAUSS if gaussian else MODEL_HE3), np.dtype(np.complex64), (3, 2)
+    raise TypeError(f"unsupported model {type(model).__name__}")
+
+
+def lpt_work_lists(costs, n_clusters):
+    """Longest-processing-time assignment of replicas to clusters (CSR lists)."""
+    order = np.argsort(-np.asarray(costs, dtype=np.float64), kind="stable")
+    heap = [(0.0, k) for k in range(n_clusters)]
+    lists = [[] for _ in range(n_clusters)]
+    for r in order:
+        load, k = heapq.heappop(heap)
+        lists[k].append(int(r))
+        heapq.heappush(heap, (load + float(costs[r]), k))
+    ptrs = np.zeros(n_clusters + 1, dtype=np.int32)
+    ptrs[1:] = np.cumsum([len(x) for x in lists])
+    idx = np.asarray([r for x in lists for r in x], dtype=np.int32)
+    loads = np.zeros(n_clusters)
+    for k, x in enumerate(lists):
+        loads[k] = sum(costs[r] for r in x)
+    return ptrs, idx, loads
+
+
+def _validate_ladder(L, temperatures, pt):
+    if L < 4 or L % 2:
+        raise ValueError("L must be even and >= 4")
+    t = np.asarray(temperatures, dtype=np.float64)
+    if t.ndim != 1 or len(t) == 0:
+        raise ValueError("Temperatures must be a nonempty 1D array")
+    if not np.all(np.isfinite(t) & (t > 0)):
+        raise ValueError("Temperatures must be positive and finite")
+    if pt:
+        if len(t) < 2:
+            raise ValueError("Parallel tempering requires at least two temperatures")
+        b = (1.0 / t).astype(np.float32)
+        if not np.all(np.diff(b) < 0):
+            raise ValueError("PT temperatures must have distinct, finite positive float32 betas")
+    return t
+
+
+class LadderBatch:
+    """Replicas of one model over ladders ``[(L, temperatures), ...]``.
+
+    Parameters mirror the drop-in classes: per-ladder ``seeds`` (site RNG,
+    default ``42 + L``, made distinct per ladder) and ``exchange_seeds``
+    (default ``seed + 1``); ``exchange_interval=None`` disables replica
+    exchange.  ``proposal`` selects the XY move ("uniform" or "gaussian" with
+    per-temperature widths starting at ``sigma0``); ``gaussian`` selects the
+    He3 conditional Gaussian sampler.
+    """
+
+    def __init__(self, model, ladders, seeds=None, exchange_interval=10, exchange_seeds=None,
+                 proposal="uniform", sigma0=1.0, gaussian=False, rho=-0.9, proposal_mass=0.0,
+                 cluster_size=None, threads=None, initial_states=None):
+        self.model = model
+        self.model_id, self.dtype, self.site_shape = _model_info(model, gaussian)
+        self.channels = CHANNELS[self.model_id]
+        self.pt = exchange_interval is not None
+        if self.pt and (isinstance(exchange_interval, bool) or int(exchange_interval) != exchange_interval
+                        or exchange_interval < 1):
+            raise ValueError("exchange_interval must be a positive integer")
+        self.exchange_interval = int(exchange_interval) if self.pt else None
+        self.ladders = [(int(L), _validate_ladder(int(L), T, self.pt)) for L, T in ladders]
+        if not self.ladders:
+            raise ValueError("need at least one ladder")
+        n_l = len(self.ladders)
+        if seeds is None:
+            seen = {}
+            seeds = []
+            for L, _ in self.ladders:
+                k = seen.get(L, 0)
+                seen[L] = k + 1
+                seeds.append(42 + L + 100003 * k)
+        self.seeds = [int(s) for s in seeds]
+        if len(self.seeds) != n_l:
+            raise ValueError("one seed per ladder")
+        self.exchange_seeds = ([s + 1 for s in self.seeds] if exchange_seeds is None
+                               else [int(s) for s in exchange_seeds])
+        self.proposal = proposal
+        if self.model_id == MODEL_XY and proposal not in ("uniform", "gaussian"):
+            raise ValueError("proposal must be 'uniform' or 'gaussian'")
+
+        # ---------------------------------------------------------- replica table
+        rows, starts, sizes, offset = [], [], [], 0
+        self.ref_offsets = []
+        for k, (L, T) in enumerate(self.ladders):
+            start = len(rows)
+            starts.append(start)
+            sizes.append(len(T))
+            for _ in range(len(T)):
+                rows.append((L, k, start, len(T), offset))
+                self.ref_offsets.append(offset)
+                offset += L * L
+        self.n_sites = offset
+        self.R = len(rows)
+        self.table_host = np.array(rows, dtype=REPLICA_DTYPE)
+        self.table = to_device(self.table_host)
+        self.ladder_starts_host = np.asarray(starts, np.int32)
+        self.ladder_sizes_host = np.asarray(sizes, np.int32)
+        self.ladder_starts = to_device(self.ladder_starts_host)
+        self.ladder_sizes = to_device(self.ladder_sizes_host)
+        self.ref_offsets_dev = to_device(np.asarray(self.ref_offsets, np.int64))
+        self.max_L = int(self.table_host["L"].max())
+        self.temperatures = np.concatenate([T for _, T in self.ladders])
+
+        # ---------------------------------------------------------- device buffers
+        site = int(np.prod(self.site_shape, dtype=np.int64))
+        self.elem_bytes = self.dtype.itemsize * site
+        self.state = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
+        self.rng = DeviceArray((self.n_sites,), XOROSHIRO128P_DTYPE)
+        ref_state = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
+        ref_rng = DeviceArray((self.n_sites,), XOROSHIRO128P_DTYPE)
+        for k, (L, T) in enumerate(self.ladders):
+            o = self.ref_offsets[starts[k]]
+            n = len(T) * L * L
+            init = (np.asarray(model.initialize_state(L, len(T), self.seeds[k]))
+                    if initial_states is None else np.asarray(initial_states[k]))
+            if init.shape != (len(T), L, L) + self.site_shape:
+                raise ValueError(f"initial state of ladder {k} has shape {init.shape}")
+            ref_state[o:o + n].copy_to_device(init.reshape((n,) + self.site_shape))
+            sub = create_xoroshiro128p_states(n, self.seeds[k])
+            ref_rng[o:o + n].raw().copy_(sub.raw())
+        self._permute(ref_state, self.state, self.elem_bytes, 0)
+        self._permute(ref_rng, self.rng, 16, 0)
+        del ref_state, ref_rng
+
+        self.betas = to_device((1.0 / self.temperatures).astype(np.float32))
+        self._initial_betas = (1.0 / self.temperatures).astype(np.float32)
+        local = np.concatenate([np.arange(n, dtype=np.int32) for n in sizes])
+        self.w2t = to_device(local)
+        self.t2w = to_device(local)
+        self.e_run = device_zeros(2 * self.R, np.float32)
+        self.energies = device_zeros(self.R, np.float64)
+        self.accepted = device_zeros(self.R, np.int64)
+        self.accepted_prev = device_zeros(self.R, np.int64)
+        self.counters = device_zeros((3, self.R), np.int64)
+        self.clock = device_zeros(2, np.int64)
+        self.drift = device_zeros(self.R, np.float64)
+        self.sigma_t = to_device(np.full(self.R, sigma0, np.float32))
+        self.staging = device_zeros((len(self.channels), self.R), np.float64)
+        self.aux = (DeviceArray((self.n_sites, 2), np.float32)
+                    if self.model_id in (MODEL_XY, MODEL_KAWAMURA) else None)
+        self.sweeps = 0
+        self.exchange_rounds = 0
+
+        if self.pt:
+            n_pairs = self.R - n_l
+            pair_rng = DeviceArray((n_pairs,), XOROSHIRO128P_DTYPE)
+            for k, n in enumerate(sizes):
+                sub = create_xoroshiro128p_states(n - 1, self.exchange_seeds[k])
+                po = starts[k] - k
+                pair_rng[po:po + n - 1].raw().copy_(sub.raw())
+            self.pair_rng = pair_rng
+            self.swap_counts = device_zeros((3, n_pairs), np.int64)
+            trips = np.zeros((5, self.R), np.int64)
+            trips[0] = -1
+            trips[2] = -1
+            for k, n in enumerate(sizes):
+                s0 = starts[k]
+                trips[0, s0] = 0
+                trips[0, s0 + n - 1] = n - 1
+                trips[2, s0] = 0
+                trips[2, s0 + n - 1] = 0
+            self.trips = to_device(trips)
+
+        # He3 parameters
+        self.coefficients = np.zeros(5, np.float32)
+        self.K = self.g_d = 0.0
+        if self.model_id in (MODEL_HE3, MODEL_HE3_GAUSS):
+            self.coefficients[:] = np.asarray(model.betas, np.float32)
+            self.K, self.g_d = float(model.K), float(model.g_d)
+        self.rho, self.mass = float(np.float32(rho)), float(np.float32(proposal_mass))
+
+        self.samples = None
+        self.n_slots = 0
+        self.first_sample_sweep = 0
+        self.sample_interval = 0
+        self._graphs = {}
+        self.configure(cluster_size, threads)
+        self.refresh_aux()
+        self.recompute_energy()
+
+    # ------------------------------------------------------------ layout
+    def _permute(self, src, dst, elem_bytes, direction):
+        _lib.call("mcgb_batch_permute", ptr(src), ptr(dst), int(elem_bytes), ptr(self.table),
+                  ptr(self.ref_offsets_dev), self.R, self.max_L, direction, _lib.stream_handle())
+
+    def ladder_state(self, k):
+        """Reference-layout state (n_temps, L, L, ...) of ladder k, walker order."""
+        L, T = self.ladders[k]
+        ref = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
+        self._permute(self.state, ref, self.elem_bytes, 1)
+        o = self.ref_offsets[self.ladder_starts_host[k]]
+        n = len(T) * L * L
+        return ref[o:o + n].copy_to_host().reshape((len(T), L, L) + self.site_shape)
+
+    def set_ladder_state(self, k, values):
+        """Overwrite ladder k's state from a reference-layout array; refreshes energies."""
+        L, T = self.ladders[k]
+        values = np.ascontiguousarray(values, dtype=self.dtype)
+        if values.shape != (len(T), L, L) + self.site_shape:
+            raise ValueError("state shape does not match the ladder")
+        ref = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
+        self._permute(self.state, ref, self.elem_bytes, 1)
+        o = self.ref_offsets[self.ladder_starts_host[k]]
+        n = len(T) * L * L
+        ref[o:o + n].copy_to_device(values.reshape((n,) + self.site_shape))
+        self._permute(ref, self.state, self.elem_bytes, 0)
+        self.refresh_aux()
+        self.recompute_energy()
+
+    def ladder_rng(self, k):
+        """Reference-layout RNG streams of ladder k as an (n, 2) uint64 array."""
+        L, T = self.ladders[k]
+        ref = DeviceArray((self.n_sites,), XOROSHIRO128P_DTYPE)
+        self._permute(self.rng, ref, 16, 1)
+        o = self.ref_offsets[self.ladder_starts_host[k]]
+        n = len(T) * L * L
+        h = ref[o:o + n].copy_to_host()
+        return np.stack([h["s0"], h["s1"]], axis=1)
+
+    # ------------------------------------------------------------ launch shape
+    def _smem(self, C):
+        npl = max(int(L) * int(L) // (4 * C) for L in self.table_host["L"])
+        return int(_lib.load().mcgb_batch_smem_bytes(self.model_id, npl))
+
+    def candidate_shapes(self):
+        """(cluster_size, threads) pairs valid for every replica of the batch."""
+        out = []
+        Ls = self.table_host["L"]
+        for C in (1, 2, 4, 8, 16):
+            if np.any(Ls % (2 * C)):
+                continue
+            smem = self._smem(C)
+            if smem > 232448:
+                continue
+            npl_max = int(self.max_L) ** 2 // (4 * C)
+            for T in (128, 256, 512, 1024):
+                if T > 32 * ((npl_max + 31) // 32) and T > 128:
+                    continue
+                out.append((C, T))
+        return out
+
+    def max_clusters(self, C, T):
+        n = ctypes.c_int(0)
+        _lib.call("mcgb_batch_max_clusters", self.model_id, C, T, self._smem(C), ctypes.byref(n))
+        return n.value
+
+    def configure(self, cluster_size=None, threads=None):
+        """Choose the cluster shape (heuristic unless given) and build work lists."""
+        if cluster_size is None or threads is None:
+            best = None
+            for C, T in self.candidate_shapes():
+                if cluster_size is not None and C != cluster_size:
+                    continue
+                if threads is not None and T != threads:
+                    continue
+                m = self.max_clusters(C, T)
+                if m < 1:
+                    continue
+                ncl = min(m, self.R)
+                # Estimated window time ~ (largest cluster load) / threads.
+                costs = self.table_host["L"].astype(np.float64) ** 2 / C
+                _, _, loads = lpt_work_lists(costs, ncl)
+                npl = int(self.max_L) ** 2 // (4 * C)
+                occupancy = min(1.0, npl / T)
+                score = loads.max() / (T * occupancy) + 0.02 * C
+                if best is None or score < best[0]:
+                    best = (score, C, T)
+            if best is None:
+                raise ValueError("no cluster shape fits this batch")
+            _, cluster_size, threads = best
+        if np.any(self.table_host["L"] % (2 * int(cluster_size))):
+            raise ValueError(f"every L must be a multiple of 2 * cluster_size = {2 * int(cluster_size)}")
+        if self._smem(int(cluster_size)) > 232448:
+            raise ValueError("a strip does not fit in shared memory; use a larger cluster_size")
+        self.cluster_size, self.threads = int(cluster_size), int(threads)
+        m = self.max_clusters(self.cluster_size, self.threads)
+        if m < 1:
+            raise ValueError(f"cluster shape ({cluster_size}, {threads}) cannot be resident")
+        self.n_clusters = min(m, self.R)
+        costs = self.table_host["L"].astype(np.float64) ** 2
+        wp, wi, _ = lpt_work_lists(costs, self.n_clusters)
+        self.work_ptr, self.work_idx = to_device(wp), to_device(wi)
+        self._graphs.clear()
+
+    # ------------------------------------------------------------ argument blocks
+    def _window(self, n_sweeps, staging=False):
+        w = BatchWindow()
+        w.table = self.table.ptr
+        w.host_table = self.table_host.ctypes.data
+        w.n_replicas = self.R
+        w.work_ptr, w.work_idx = self.work_ptr.ptr, self.work_idx.ptr
+        w.n_clusters, w.cluster_size, w.threads = self.n_clusters, self.cluster_size, self.threads
+        w.state, w.rng, w.betas, w.w2t = self.state.ptr, self.rng.ptr, self.betas.ptr, self.w2t.ptr
+        w.aux = None if self.aux is None else self.aux.ptr
+        w.e_run, w.energies, w.accepted = self.e_run.ptr, self.energies.ptr, self.accepted.ptr
+        w.counters = self.counters.ptr if self.model_id == MODEL_HE3_GAUSS else None
+        if self.samples is not None:
+            w.samples = self.samples.ptr
+            w.staging = self.staging.ptr if (staging and self.pt) else None
+            w.n_temps_total = self.R
+            w.n_slots = self.n_slots
+            w.first_sample_sweep = self.first_sample_sweep
+            w.sample_interval = self.sample_interval
+        w.clock = self.clock.ptr
+        w.n_sweeps = int(n_sweeps)
+        w.J = float(getattr(self.model, "J", 1.0))
+        w.delta = float(getattr(self.model, "delta", 0.0))
+        w.sigma_t = self.sigma_t.ptr if (self.model_id == MODEL_XY and self.proposal == "gaussian") else None
+        for q in range(5):
+            w.coefficients[q] = float(self.coefficients[q])
+        w.K, w.g_d, w.rho, w.mass = self.K, self.g_d, self.rho, self.mass
+        return w
+
+    def _pt(self):
+        p = BatchPT()
+        p.t2w, p.rng = self.t2w.ptr, self.pair_rng.ptr
+        p.swap_counts, p.trips = self.swap_counts.ptr, self.trips.ptr
+        p.ladder_starts, p.ladder_sizes = self.ladder_starts.ptr, self.ladder_sizes.ptr
+        p.n_ladders = len(self.ladders)
+        p.channels = len(self.channels)
+        return p
+
+    # ------------------------------------------------------------ stepping
+    def _enqueue_window(self, n_sweeps, exchange, tune=False):
+        s = _lib.stream_handle()
+        w = self._window(n_sweeps, staging=exchange)
+        self._keep = w
+        _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
+        if exchange:
+            p = self._pt()
+            _lib.call("mcgb_batch_exchange", ctypes.byref(w), ctypes.byref(p), s)
+        if tune:
+            _lib.call("mcgb_batch_tune_sigma", self.sigma_t.cptr, self.accepted.cptr, self.accepted_prev.cptr,
+                      self.w2t.cptr, self.table.cptr, self.R, int(n_sweeps), 0.5, 2.0, 0.02, 2 * np.pi, s)
+        _lib.call("mcgb_batch_clock_tick", self.clock.cptr, int(n_sweeps), int(bool(exchange)), s)
+
+    def _schedule(self, n_sweeps):
+        """Split n_sweeps into (length, exchange_after) windows aligned to the PT schedule."""
+        out = []
+        s, left = self.sweeps, n_sweeps
+        while left > 0:
+            if self.pt:
+                to_ex = self.exchange_interval - (s % self.exchange_interval)
+                n = min(left, to_ex)
+                out.append((n, n == to_ex))
+            else:
+                n = min(left, 10)
+                out.append((n, False))
+            s += n
+            left -= n
+        return out
+
+    def run(self, n_sweeps, tune=False, graph=True):
+        """Advance every replica by n_sweeps sweeps (with exchanges on schedule).
+
+        Runs of full windows replay captured CUDA graphs of up to 64 windows;
+        partial windows at the ends launch directly.
+        """
+        plan = self._schedule(int(n_sweeps))
+        full = (self.exchange_interval, True) if self.pt else (10, False)
+        i = 0
+        while i < len(plan):
+            if graph and plan[i] == full:
+                j = i
+                while j < len(plan) and plan[j] == full:
+                    j += 1
+                remaining = j - i
+                while remaining:
+                    chunk = 1 << min(6, remaining.bit_length() - 1)
+                    self._replay(chunk, full, tune)
+                    remaining -= chunk
+                i = j
+                continue
+            n, ex = plan[i]
+            self._enqueue_window(n, ex, tune)
+            self._advance(n, ex)
+            i += 1
+
+    def _advance(self, n, exchanged, times=1):
+        self.sweeps += n * times
+        if exchanged:
+            self.exchange_rounds += times
+
+    def _replay(self, count, step, tune):
+        key = (count, step, tune, self.samples is not None and self.samples.ptr)
+        g = self._graphs.get(key)
+        if g is None:
+            # Capture reads only argument blocks; the device clock advances at replay.
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                for _ in range(count):
+                    self._enqueue_window(step[0], step[1], tune)
+            self._graphs[key] = g
+        g.replay()
+        self._advance(step[0], step[1], count)
+
+    def exchange_now(self):
+        """Attempt one matching now (fresh energies from the running cache)."""
+        if not self.pt:
+            raise ValueError("this batch has no replica exchange")
+        s = _lib.stream_handle()
+        w = self._window(0)
+        _lib.call("mcgb_batch_exchange", ctypes.byref(w), ctypes.byref(self._pt()), s)
+        _lib.call("mcgb_batch_clock_tick", self.clock.cptr, 0, 1, s)
+        self.exchange_rounds += 1
+
+    def refresh_aux(self):
+        """Recompute the (cos, sin) cache from the state."""
+        if self.aux is not None:
+            w = self._window(0)
+            _lib.call("mcgb_batch_refresh_aux", self.model_id, ctypes.byref(w), _lib.stream_handle())
+
+    def recompute_energy(self):
+        """FP64 total energies; returns drift = running - exact per replica."""
+        w = self._window(0)
+        _lib.call("mcgb_batch_recompute_energy", self.model_id, ctypes.byref(w), self.drift.cptr,
+                  _lib.stream_handle())
+        return self.drift
+
+    # ------------------------------------------------------------ sampling
+    def allocate_samples(self, first_sample_sweep, sample_interval, n_slots):
+        self.samples = device_zeros((n_slots, len(self.channels), self.R), np.float64)
+        self.n_slots, self.first_sample_sweep = int(n_slots), int(first_sample_sweep)
+        self.sample_interval = int(sample_interval)
+        self._graphs.clear()
+
+    def simulate(self, thermalization_sweeps=1000, measurement_sweeps=4000, sample_interval=10,
+                 tune_sigma=None, graph=True):
+        """Simulation.run for every ladder: returns one ``{"samples", "metadata"}``
+        per ladder (core/simulation.py:28-96 schema; samples in temperature order)."""
+        if thermalization_sweeps < 0:
+            raise ValueError("Thermalization sweeps cannot be negative")
+        if measurement_sweeps < 1:
+            raise ValueError("Measurement sweeps must be positive")
+        if sample_interval < 1 or sample_interval > measurement_sweeps:
+            raise ValueError("Invalid sampling interval")
+        if tune_sigma is None:
+            tune_sigma = self.model_id == MODEL_XY and self.proposal == "gaussian"
+        start = self.sweeps
+        self.samples = None
+        self.run(thermalization_sweeps, tune=tune_sigma, graph=graph)
+        n_slots = measurement_sweeps // sample_interval
+        self.allocate_samples(start + thermalization_sweeps + sample_interval, sample_interval, n_slots)
+        self.run(measurement_sweeps, tune=False, graph=graph)
+        data = self.samples.copy_to_host()
+        sample_sweeps = thermalization_sweeps + sample_interval * np.arange(1, n_slots + 1)
+        runs = []
+        for k, (L, T) in enumerate(self.ladders):
+            s0, n = int(self.ladder_starts_host[k]), len(T)
+            samples = {name: data[:, c, s0:s0 + n].copy() for c, name in enumerate(self.channels)}
+            metadata = {
+                "L": L, "temperatures": T.copy(), "seed": self.seeds[k],
+                "model_parameters": self.model.parameters(),
+                "thermalization_sweeps": thermalization_sweeps,
+                "measurement_sweeps": measurement_sweeps,
+                "sample_interval": sample_interval,
+                "sample_sweeps": sample_sweeps.copy(),
+            }
+            if self.pt:
+                metadata["parallel_tempering"] = self.diagnostics(k)
+            runs.append({"samples": samples, "metadata": metadata})
+        self.samples = None
+        return runs
+
+    # ------------------------------------------------------------ diagnostics
+    def diagnostics(self, k):
+        """core/parallel_tempering.py:280-317 diagnostics of ladder k."""
+        counts = self.swap_counts.copy_to_host()
+        s0, n = int(self.ladder_starts_host[k]), int(self.ladder_sizes_host[k])
+        po = s0 - k
+        c = counts[:, po:po + n - 1]
+        if np.any(c[2]):
+            raise FloatingPointError("Nonfinite energies encountered during replica exchange")
+        trips = self.trips.copy_to_host()[:, s0:s0 + n]
+        w2t = self.w2t.copy_to_host()[s0:s0 + n]
+        t2w = self.t2w.copy_to_host()[s0:s0 + n]
+        attempts, accepted = c[0], c[1]
+        rates = np.divide(accepted, attempts, out=np.zeros(n - 1), where=attempts > 0)
+        completed = int(trips[3].sum())
+        return {
+            "exchange_interval": self.exchange_interval,
+            "exchange_seed": self.exchange_seeds[k],
+            "sweeps": self.sweeps,
+            "exchange_rounds": self.exchange_rounds,
+            "next_parity": (self.exchange_rounds & 1) if n > 2 else 0,
+            "diagnostics_scope": "since_wrapper_creation_including_thermalization",
+            "temperature_betas": self._initial_betas[s0:s0 + n].copy(),
+            "attempts": attempts.copy(), "accepted": accepted.copy(), "acceptance_rates": rates,
+            "walker_to_temperature": w2t, "temperature_to_walker": t2w,
+            "walker_round_trips": trips[3].copy(),
+            "walker_round_trip_total_sweeps": trips[4].copy(),
+            "mean_round_trip_sweeps": float(trips[4].sum()) / completed if completed else None,
+        }
+
+    def acceptance(self):
+        """Accepted moves per replica so far (device counters)."""
+        return self.accepted.copy_to_host()
+
+    # ------------------------------------------------------------ autotuning
+    def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False):
+        """Time each valid (cluster_size, threads) on a copy-free trial window
+        and keep the fastest.  State and RNG are saved and restored, so tuning
+        does not change the Markov chain."""
+        shapes = shapes or self.candidate_shapes()
+        n = sweeps_per_trial or (self.exchange_interval or 10)
+        saved_state = self.state.raw().clone()
+        saved_aux = None if self.aux is None else self.aux.raw().clone()
+        saved_rng = self.rng.raw().clone()
+        saved_e = self.e_run.raw().clone()
+        saved_acc = self.accepted.raw().clone()
+        saved_clock = self.clock.raw().clone()
+        saved_samples, self.samples = self.samples, None
+        results = []
+        for C, T in shapes:
+            try:
+                self.configure(C, T)
+            except ValueError:
+                continue
+            s = _lib.stream_handle()
+            w = self._window(n)
+            _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 3
+            ev0.record()
+            for _ in range(reps):
+                _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
+            ev1.record()
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1) / reps
+            results.append((ms, C, T))
+            if verbose:
+                print(f"autotune C={C} T={T}: {ms:.3f} ms per {n}-sweep window")
+        self.state.raw().copy_(saved_state)
+        if saved_aux is not None:
+            self.aux.raw().copy_(saved_aux)
+        self.rng.raw().copy_(saved_rng)
+        self.e_run.raw().copy_(saved_e)
+        self.accepted.raw().copy_(saved_acc)
+        self.clock.raw().copy_(saved_clock)
+        self.samples = saved_samples
+        results.sort()
+        _, C, T = results[0]
+        self.configure(C, T)
+        self.recompute_energy()
+        return results
+
+
+def smoke_run():
+    """A short batched XY run with exchanges, compared with an FP64 recompute."""
+    from ..models.xy.model import XYModel
+
+    b = LadderBatch(XYModel(), [(16, np.geomspace(0.7, 1.2, 4)), (32, np.geomspace(0.7, 1.2, 4))],
+                    exchange_interval=5, proposal="gaussian")
+    b.run(20)
+    e = b.energies.copy_to_host()
+    drift = b.recompute_energy().copy_to_host()
+    if not np.all(np.isfinite(e)) or np.max(np.abs(drift)) > 1e-3 * np.max(np.abs(e)):
+        raise AssertionError("batched XY energy drift too large")
+    b.diagnostics(0)

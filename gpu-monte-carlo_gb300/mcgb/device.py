@@ -86,12 +86,19 @@ class DeviceArray:
         }
 
     # ------------------------------------------------------------ views
+    def raw(self):
+        """The array's bytes as a flat uint8 torch tensor (no copy)."""
+        return self._t[: self._nbytes]
+
     def torch(self, dtype=None):
-        """Typed torch view of the same memory (no copy)."""
+        """Typed torch view of the same memory (no copy); array-shaped when the
+        element size matches, else flat."""
         if dtype is None:
             dtype = _TORCH_DTYPES[self.dtype]
-        raw = self._t[: self._nbytes]
-        return raw.view(dtype).view(self.shape) if self.dtype.fields is None else raw.view(dtype)
+        view = self.raw().view(dtype)
+        if self.dtype.fields is None and view.element_size() == self.dtype.itemsize:
+            return view.view(self.shape)
+        return view
 
     def __getitem__(self, key):
         """Contiguous slices along axis 0 (``chunk[:used]``, ``arr[3]``)."""

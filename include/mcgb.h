@@ -160,6 +160,131 @@ int mcgb_pt_exchange(const double *energies, float *betas, int32_t *walker_to_te
 int mcgb_pt_record_walkers(const int32_t *walker_to_temperature, const int32_t *walker_ids,
                            int32_t *history_row, int n, void *stream);
 
+/* ------------------------------------------------------------ Batched engine
+ * No single reference counterpart: these run what the reference does with
+ * one Runtime per (L, ladder) and four launches per sweep
+ * (core/runtime.py:87-99, core/parallel_tempering.py:245-269,
+ * core/simulation.py:36-72) as one launch per exchange window over a table
+ * of replicas of any mix of L.  Inside a window the lattice of each replica
+ * lives in the shared memory of one thread-block cluster (one strip of rows
+ * per CTA) and its RNG streams in registers.
+ *
+ * Batch layout ("colour-major"): per replica, four planes (one per
+ * checkerboard colour c = 2*(i%2) + j%2) of (L/2) x (L/2) sites each; the
+ * RNG array has one 16-byte stream per site in the same order.  The
+ * permutation kernels below convert from/to the reference layout, keeping
+ * each site's stream. */
+
+enum {
+    MCGB_MODEL_ISING = 0,
+    MCGB_MODEL_XY = 1,
+    MCGB_MODEL_KAWAMURA = 2,
+    MCGB_MODEL_HE3 = 3,       /* Cartesian proposals */
+    MCGB_MODEL_HE3_GAUSS = 4, /* conditional Gaussian MH proposals */
+};
+
+typedef struct mcgb_replica {
+    int32_t L;             /* even; divisible by 2 * cluster_size */
+    int32_t ladder;        /* ladder index */
+    int32_t ladder_start;  /* first replica index (= temperature slot 0) of the ladder */
+    int32_t n_temps;       /* replicas in the ladder */
+    int64_t state_offset;  /* first site of the replica in the batch arrays */
+} mcgb_replica;
+
+typedef struct mcgb_batch_window {
+    const mcgb_replica *table;      /* device, n_replicas entries */
+    const mcgb_replica *host_table; /* host copy (validated on every call) */
+    int32_t n_replicas;
+    const int32_t *work_ptr;        /* device, n_clusters + 1: cluster k runs */
+    const int32_t *work_idx;        /*   work_idx[work_ptr[k] .. work_ptr[k+1]) */
+    int32_t n_clusters, cluster_size, threads;
+    void *state;                    /* colour-major: int8 / float / 5 floats / 6 complex64 per site */
+    void *rng;                      /* colour-major 16-byte streams */
+    void *aux;                      /* XY, Kawamura: colour-major (cos theta, sin theta) float pairs
+                                       kept with the state so every window sees the values the
+                                       updates computed; NULL for other models */
+    const float *betas;             /* per replica, walker order */
+    const int32_t *w2t;             /* per replica: temperature slot within its ladder */
+    float *e_run;                   /* 2 per replica: compensated running energy (hi, lo) */
+    double *energies;               /* out, per replica: energy after the window */
+    long long *accepted;            /* per replica: += accepted moves (He3: all sub-counters) */
+    long long *counters;            /* He3 Gaussian: (3, n_replicas) attempts/accepted/nonfinite, else NULL */
+    double *samples;                /* [n_slots][channels][n_temps_total] or NULL */
+    double *staging;                /* [channels][n_replicas]: when not NULL, a sample due at the
+                                       window's last sweep goes here (walker order) for the exchange
+                                       to scatter with the updated temperature map */
+    int32_t n_temps_total, n_slots;
+    const int64_t *clock;           /* device {sweeps completed, exchange rounds} before the window */
+    int64_t first_sample_sweep;     /* cumulative sweep number of sample slot 0 */
+    int32_t sample_interval;        /* 0 = no samples */
+    int32_t n_sweeps;               /* sweeps in this window */
+    float J, delta;                 /* Ising/XY/Kawamura coupling, uniform proposal width */
+    const float *sigma_t;           /* XY: Gaussian width per temperature slot (NULL = uniform delta) */
+    float coefficients[5], K, g_d, rho, mass; /* He3 */
+} mcgb_batch_window;
+
+/* Number of float64 sample channels a model writes per replica. */
+int mcgb_batch_channels(int model);
+/* Dynamic shared memory (bytes) a window needs for a strip of
+ * max_plaquettes = max(L^2) / (4 * cluster_size). */
+int64_t mcgb_batch_smem_bytes(int model, int64_t max_plaquettes);
+/* Largest number of co-resident clusters of `cluster_size` CTAs of `threads`
+ * threads with `smem_bytes` dynamic shared memory (cudaOccupancyMaxActiveClusters). */
+int mcgb_batch_max_clusters(int model, int cluster_size, int threads, int64_t smem_bytes, int *out);
+/* One window of n_sweeps sweeps over every replica of the batch. */
+int mcgb_batch_window_run(int model, const mcgb_batch_window *w, void *stream);
+/* Reference layout <-> colour-major, elem_bytes per site (a multiple of 1, 4
+ * or 16), for every replica of the table (device) with n_replicas entries and
+ * max_L the largest L.  direction 0: reference -> batch, 1: batch -> reference.
+ * `ref_offsets` (device, int64 per replica) gives each replica's first site in
+ * the reference-layout array. */
+int mcgb_batch_permute(const void *src, void *dst, int64_t elem_bytes, const mcgb_replica *table,
+                       const int64_t *ref_offsets, int n_replicas, int max_L, int direction,
+                       void *stream);
+/* Recompute the (cos, sin) cache `aux` from the state (after the state was
+ * written from outside a window). */
+int mcgb_batch_refresh_aux(int model, const mcgb_batch_window *w, void *stream);
+/* FP64 total energy of every replica from the colour-major state (the
+ * periodic drift check): writes energies[r], drift[r] = running - exact, and
+ * resets e_run[r] to the exact value. */
+int mcgb_batch_recompute_energy(int model, const mcgb_batch_window *w, double *drift, void *stream);
+/* Parallel-tempering bookkeeping of a batch: per ladder l, replicas
+ * [ladder_starts[l], ladder_starts[l] + ladder_sizes[l]); t2w holds, per
+ * ladder slot, the walker index local to the ladder (w2t in the window block
+ * holds the slot per replica); rng has one stream per neighbouring pair
+ * (pair index = ladder_start - l + left); swap_counts is (3, n_pairs_total),
+ * trips (5, n_replicas). */
+typedef struct mcgb_batch_pt {
+    int32_t *t2w;
+    void *rng;
+    int64_t *swap_counts;
+    int64_t *trips;
+    const int32_t *ladder_starts;
+    const int32_t *ladder_sizes;
+    int32_t n_ladders;
+    int32_t channels;               /* sample channels of the model (staging rows) */
+} mcgb_batch_pt;
+
+/* Replica exchange for every ladder (one thread block per ladder,
+ * core/parallel_tempering.py:35-91 per ladder) after a window described by
+ * `w` (energies, betas, w2t, clock, n_sweeps; samples/staging for the
+ * deferred window-end sample).  The trip sweep is clock[0] + n_sweeps and the
+ * matching parity of a ladder with more than two replicas is clock[1] % 2
+ * (two-replica ladders always use 0), as core/parallel_tempering.py:245-269
+ * schedules them.  A staged window-end sample is then written to the slots
+ * of the updated map, matching a measurement taken after the exchange. */
+int mcgb_batch_exchange(const mcgb_batch_window *w, const mcgb_batch_pt *pt, void *stream);
+/* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
+ * a captured graph of windows and exchanges can be replayed. */
+int mcgb_batch_clock_tick(int64_t *clock, int n_sweeps, int exchanged, void *stream);
+/* Robbins-Monro step of the per-temperature Gaussian widths towards a target
+ * acceptance: sigma_t[slot] *= exp(gain * (rate - target)), clamped to
+ * [lo, hi], rate = (accepted - accepted_prev) / (L^2 * n_sweeps) of the
+ * replica at that slot; then accepted_prev = accepted. */
+int mcgb_batch_tune_sigma(float *sigma_t, const long long *accepted, long long *accepted_prev,
+                          const int32_t *w2t, const mcgb_replica *table, int n_replicas, int n_sweeps,
+                          float target, float gain, float lo, float hi, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

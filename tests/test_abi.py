@@ -1,0 +1,58 @@
+"""The C ABI: every function include/mcgb.h declares is exported by
+libmcgb.so and bound by the ctypes layer; no GPU needed (no compute calls)."""
+
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "mcgb.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mcgb_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mcgb import _lib
+    return _lib.load()
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    assert "mcgb_rng_init" in names and "mcgb_batch_window_run" in names
+    assert len(names) >= 30
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from mcgb import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.lib_path())], capture_output=True, text=True)
+    exported = set(re.findall(r"\bT (mcgb_[a-z0-9_]+)$", out.stdout, flags=re.M))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_ctypes_layer_binds_every_declared_symbol(lib):
+    from mcgb import _lib
+    bound = set(_lib.SIGNATURES) | {"mcgb_last_error", "mcgb_version"}
+    missing = [n for n in declared_functions() if n not in bound]
+    assert not missing, f"declared but not bound in mcgb._lib: {missing}"
+    for name in declared_functions():
+        assert getattr(lib, name) is not None
+
+
+def test_argument_validation_without_a_gpu(lib):
+    """Invalid sizes are rejected on the host before any CUDA call."""
+    from mcgb import _lib
+    assert lib.mcgb_ising_update_color(None, None, None, 1, 5, 0, ctypes.c_float(1.0), None) == _lib.EINVAL
+    assert "L must be even" in _lib.last_error()
+    assert lib.mcgb_pt_exchange(None, None, None, None, None, None, None, 1, 0, 0, None) == _lib.EINVAL
+    assert lib.mcgb_batch_channels(1) == 5 and lib.mcgb_batch_channels(4) == 10
+    assert lib.mcgb_batch_channels(9) == _lib.EINVAL
+    assert lib.mcgb_version().decode().startswith("mcgb")

@@ -1,0 +1,178 @@
+"""Batched ladder engine against the per-colour drop-in path and the oracle."""
+
+from unittest.mock import patch  # noqa: F401
+
+import numpy as np
+import pytest
+
+import npref
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def dropin_ising(L, temps, seed, init):
+    from mcgb.core.runtime import Runtime
+    from mcgb.models.ising.model import IsingModel
+    rt = Runtime(IsingModel(J=1.0), L, temps, seed=seed)
+    rt.state.copy_to_device(init)
+    return rt
+
+
+def seeded_spins(rng, R, L):
+    return rng.choice(np.array([-1, 1], dtype=np.int8), (R, L, L))
+
+
+@pytest.mark.parametrize("cluster_size,threads", [(1, 256), (2, 512), (4, 1024), (8, 128)])
+def test_ising_batch_bit_exact_with_dropin_runtime(cluster_size, threads):
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    L, temps = 64, [1.5, 2.269, 3.0]
+    rng = np.random.default_rng(106)
+    inits = [seeded_spins(rng, 1, L) for _ in temps]
+    b = LadderBatch(IsingModel(), [(L, [T]) for T in temps], seeds=[42 + L] * 3, exchange_interval=None,
+                    cluster_size=cluster_size, threads=threads, initial_states=inits)
+    b.run(100)
+    for k, T in enumerate(temps):
+        rt = dropin_ising(L, [T], 42 + L, inits[k])
+        for _ in range(100):
+            rt.sweep()
+        np.testing.assert_array_equal(b.ladder_state(k), rt.snapshot())
+        rs = rt.rng_states.copy_to_host()
+        np.testing.assert_array_equal(b.ladder_rng(k), np.stack([rs["s0"], rs["s1"]], axis=1))
+    e = b.energies.copy_to_host()
+    for k in range(3):
+        np.testing.assert_array_equal(e[k], oracle.ising_energy(b.ladder_state(k), np.float32(1))[0])
+
+
+def test_ising_batch_pt_simulation_equals_dropin_simulation():
+    """Same seeds: identical samples, maps and swap counters to Simulation(ParallelTempering)."""
+    from mcgb.batch import LadderBatch
+    from mcgb.core.parallel_tempering import ParallelTempering
+    from mcgb.core.runtime import Runtime
+    from mcgb.core.simulation import Simulation
+    from mcgb.models.ising.model import IsingModel
+    L, temps = 16, np.geomspace(1.8, 3.0, 5)
+    init = seeded_spins(np.random.default_rng(5), 5, L)
+    b = LadderBatch(IsingModel(), [(L, temps), (16, temps[:4])], seeds=[58, 77], exchange_interval=3,
+                    exchange_seeds=[59, 78], cluster_size=2, threads=128,
+                    initial_states=[init, init[:4].copy()])
+    runs = b.simulate(thermalization_sweeps=7, measurement_sweeps=40, sample_interval=2)
+    for k, (init_k, T_k, seed) in enumerate(((init, temps, 58), (init[:4].copy(), temps[:4], 77))):
+        rt = Runtime(IsingModel(), L, T_k, seed=seed)
+        rt.state.copy_to_device(init_k)
+        pt = ParallelTempering(rt, exchange_interval=3, seed=seed + 1)
+        ref = Simulation(pt, thermalization_sweeps=7, measurement_sweeps=40, sample_interval=2).run()
+        for name in ref["samples"]:
+            np.testing.assert_array_equal(runs[k]["samples"][name], ref["samples"][name], err_msg=name)
+        np.testing.assert_array_equal(runs[k]["metadata"]["sample_sweeps"], ref["metadata"]["sample_sweeps"])
+        d, dr = runs[k]["metadata"]["parallel_tempering"], ref["metadata"]["parallel_tempering"]
+        for key in ("attempts", "accepted", "walker_to_temperature", "temperature_to_walker",
+                    "walker_round_trips", "walker_round_trip_total_sweeps", "exchange_rounds", "sweeps"):
+            np.testing.assert_array_equal(d[key], dr[key], err_msg=key)
+        np.testing.assert_array_equal(b.ladder_state(k), rt.snapshot())
+
+
+def test_graph_replay_equals_direct_launches():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+    kw = dict(seeds=[3], exchange_interval=5, proposal="gaussian", cluster_size=2, threads=256)
+    a = LadderBatch(XYModel(), [(32, np.geomspace(0.7, 1.2, 6))], **kw)
+    c = LadderBatch(XYModel(), [(32, np.geomspace(0.7, 1.2, 6))], **kw)
+    a.run(60, graph=True)
+    c.run(60, graph=False)
+    np.testing.assert_array_equal(a.ladder_state(0), c.ladder_state(0))
+    np.testing.assert_array_equal(a.w2t.copy_to_host(), c.w2t.copy_to_host())
+    np.testing.assert_array_equal(a.clock.copy_to_host(), [60, 12])
+
+
+@pytest.mark.parametrize("proposal", ["uniform", "gaussian"])
+def test_xy_batch_window_matches_oracle(proposal):
+    """One 1-sweep window per colour order against the oracle: RNG bit-exact,
+    angles within float32 rounding except rare acceptance flips."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+    L, temps = 32, np.array([0.7, 0.9, 1.1, 1.2])
+    init = np.random.default_rng(6).uniform(-np.pi, np.pi, (4, L, L)).astype(np.float32)
+    b = LadderBatch(XYModel(), [(L, temps)], seeds=[5], exchange_interval=None, proposal=proposal,
+                    sigma0=1.1, cluster_size=4, threads=128, initial_states=[init])
+    b.run(1)
+    ref, rr = init.copy(), oracle.rng_states(4 * L * L, 5)
+    betas = (1 / temps).astype(np.float32)
+    for c in range(4):
+        if proposal == "uniform":
+            oracle.xy_update_color(ref, rr, betas, c, np.float32(1), np.float32(1.5))
+        else:
+            oracle.xy_update_color_gauss(ref, rr, betas, np.full(4, 1.1, np.float32), c, np.float32(1))
+    np.testing.assert_array_equal(b.ladder_rng(0), rr)
+    got = b.ladder_state(0)
+    d = np.abs(np.angle(np.exp(1j * (got.astype(np.float64) - ref))))
+    assert np.mean(d > 1e-4) <= 1e-3
+
+
+def test_xy_running_energy_tracks_fp64_recompute():
+    """Single-sweep energy differences agree with an FP64 recompute within 1e-5 relative."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+    L, temps = 64, np.geomspace(0.7, 1.2, 8)
+    init = np.random.default_rng(9).uniform(-np.pi, np.pi, (8, L, L)).astype(np.float32)
+    b = LadderBatch(XYModel(), [(L, temps)], exchange_interval=1, proposal="gaussian", initial_states=[init])
+    e0 = oracle.xy_energy(init, np.float32(1))
+    np.testing.assert_allclose(b.energies.copy_to_host(), e0, rtol=1e-12)
+    b.run(1)
+    after = b.ladder_state(0)
+    e1_exact = oracle.xy_energy(after, np.float32(1))
+    e1_run = b.energies.copy_to_host()
+    d_run, d_exact = e1_run - e0, e1_exact - e0
+    assert np.all(np.abs(d_run - d_exact) <= 1e-5 * np.abs(d_exact))
+    b.run(200)
+    e_run = b.energies.copy_to_host()
+    drift = b.recompute_energy().copy_to_host()
+    exact = oracle.xy_energy(b.ladder_state(0), np.float32(1))
+    np.testing.assert_allclose(b.energies.copy_to_host(), exact, rtol=1e-10)
+    assert np.all(np.abs(drift) <= 1e-5 * np.abs(exact))
+    np.testing.assert_allclose(e_run - drift, exact, rtol=1e-10)
+
+
+def test_xy_batch_samples_match_exact_observables():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+    L, temps = 32, np.geomspace(0.7, 1.2, 4)
+    b = LadderBatch(XYModel(), [(L, temps)], exchange_interval=4, proposal="gaussian", cluster_size=2,
+                    threads=256)
+    runs = b.simulate(thermalization_sweeps=10, measurement_sweeps=8, sample_interval=8)
+    last = {k: v[-1] for k, v in runs[0]["samples"].items()}
+    state = b.ladder_state(0)
+    ref = npref.xy(state, 1.0)
+    order = b.w2t.copy_to_host()
+    for name in ref:
+        got = np.empty(4)
+        got[order] = ref[name]
+        np.testing.assert_allclose(last[name], got, rtol=1e-5, atol=2e-3 * L, err_msg=name)
+
+
+def test_ragged_batch_ladders_match_their_own_runtimes():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    ladders = [(16, [2.0, 2.5]), (32, [2.0, 2.5]), (64, [2.2, 2.6])]
+    rng = np.random.default_rng(1)
+    inits = [seeded_spins(rng, 2, L) for L, _ in ladders]
+    b = LadderBatch(IsingModel(), ladders, seeds=[10, 20, 30], exchange_interval=None, initial_states=inits)
+    assert b.cluster_size in (1, 2, 4, 8)
+    b.run(30)
+    for k, (L, T) in enumerate(ladders):
+        rt = dropin_ising(L, T, [10, 20, 30][k], inits[k])
+        for _ in range(30):
+            rt.sweep()
+        np.testing.assert_array_equal(b.ladder_state(k), rt.snapshot())
+
+
+def test_invalid_batches_raise():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    with pytest.raises(ValueError):
+        LadderBatch(IsingModel(), [(6, [1.0, 1.0])])
+    with pytest.raises(ValueError):
+        LadderBatch(IsingModel(), [(16, [2.0])], exchange_interval=10)
+    with pytest.raises(ValueError):
+        LadderBatch(IsingModel(), [(16, [2.0, 3.0])], cluster_size=16, threads=128)
