@@ -1,0 +1,440 @@
+"""Throughput of the lattice Monte Carlo hot path: attempted spin updates/ns.
+
+Workload (one GPU): the XY parallel-tempering ladder -- L=128 periodic
+square lattice, J=1, 32 temperatures geometric in [0.70, 1.20], angles drawn
+uniformly in [0, 2pi) from a seed (wrapped to [-pi, pi)), Gaussian Metropolis
+proposals with per-temperature widths tuned to ~50% acceptance during warm-up,
+a replica exchange every 10 sweeps and a sample of (E, mx, my, twist cos/sin)
+every 10 sweeps.  One step = 100 sweeps of all 32 replicas
+(52,428,800 attempted updates).
+
+Arms:
+  default           the batched mixed-precision engine (mcgb.batch.LadderBatch),
+                    one window launch per 10 sweeps, CUDA-graph replay;
+  --impl reference  the reference algorithm on the host cores: the C
+                    restatement of its kernels (the reference has no CPU sweep
+                    of its own), OpenMP over replicas, a bounded sample.
+
+Under torchrun each rank runs its own independent ladder (seeded by rank):
+ladders share nothing, so the work shards with no data-path collective
+(weak scaling); the timing takes the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "gpu-monte-carlo_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+L = 128
+N_TEMPS = 32
+T_MIN, T_MAX = 0.70, 1.20
+EXCHANGE_INTERVAL = 10
+SAMPLE_INTERVAL = 10
+SWEEPS_PER_STEP = 100
+BYTES_PER_UPDATE = 40      # XY: 4+4 B angle read+write, 32 B RNG stream read+write
+METRIC = "attempted spin updates/ns"
+WORKLOAD = "XY PT ladder L=128 x 32 temperatures geometric [0.70, 1.20], Gaussian MH (sigma tuned to ~50%)"
+
+
+def temperatures():
+    return np.geomspace(T_MIN, T_MAX, N_TEMPS)
+
+
+def initial_angles(seed):
+    rng = np.random.default_rng(seed)
+    theta = rng.uniform(0.0, 2 * np.pi, (N_TEMPS, L, L))
+    theta = np.where(theta >= np.pi, theta - 2 * np.pi, theta).astype(np.float32)
+    return np.clip(theta, np.float32(-np.pi), np.nextafter(np.float32(np.pi), np.float32(0)))
+
+
+def load_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU arms
+
+
+def cpu_sample(n_threads, sweeps, seed=7):
+    """Time the oracle (the reference algorithm restated in C) on the host
+    cores for `sweeps` sweeps of the ladder with exchanges; updates/ns."""
+    import oracle
+
+    temps = temperatures()
+    R = N_TEMPS
+    theta = initial_angles(seed)
+    rng = oracle.rng_states(R * L * L, seed)
+    betas = (1.0 / temps).astype(np.float32)
+    sigmas = np.full(R, 0.93, np.float32)
+    w2t = np.arange(R, dtype=np.int32)
+    t2w = np.arange(R, dtype=np.int32)
+    pair_rng = oracle.rng_states(R - 1, seed + 1)
+    counts = np.zeros((3, R - 1), np.int64)
+    trips = oracle.pt_initial_trips(R)
+    done, parity = 0, 0
+    t0 = time.perf_counter()
+    while done < sweeps:
+        n = min(EXCHANGE_INTERVAL, sweeps - done)
+        oracle.xy_sweeps(theta, rng, betas, np.float32(1.0), np.float32(1.5), n,
+                         sigmas=sigmas[w2t], n_threads=n_threads)
+        done += n
+        if n == EXCHANGE_INTERVAL:
+            e = oracle.xy_energy(theta, np.float32(1.0))
+            oracle.pt_exchange(e, betas, w2t, t2w, pair_rng, counts, trips, parity, done)
+            parity ^= 1
+            oracle.xy_measure(theta, np.float32(1.0), temperature_indices=w2t, cached=e)
+    dt = time.perf_counter() - t0
+    return R * L * L * sweeps / (dt * 1e9), dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    cores = os.cpu_count() or 1
+    sweeps = SWEEPS_PER_STEP
+    cpu_sample(cores, 10)  # warm-up pages and threads
+    vals = []
+    t_start = time.perf_counter()
+    for _ in range(args.warmup):
+        cpu_sample(cores, sweeps)
+    for _ in range(args.steps):
+        v, _ = cpu_sample(cores, sweeps)
+        vals.append(v)
+    total = time.perf_counter() - t_start
+    value = float(np.median(vals))
+    ms = N_TEMPS * L * L * sweeps / (value * 1e6)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "updates/ns",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform angles)",
+        "config": {"workload": WORKLOAD, "sweeps_per_step": sweeps, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "updates/ns", "cores": cores, "kind": "port",
+                         "sample": f"{sweeps} sweeps of the 32-replica L=128 ladder per step, exchange "
+                                   f"every 10 sweeps, {cores} OpenMP threads (the reference has no CPU "
+                                   f"sweep; this is its kernels restated in C)"},
+        "e2e": {"value": value, "unit": "updates/ns", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": total,
+    }
+    return line
+
+
+# ------------------------------------------------------------------ GPU arm
+
+
+def run_mcgb(args, rank, world):
+    import torch
+
+    import mcgb
+    from mcgb import device
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    temps = temperatures()
+    seed = 42 + L + 1000 * rank
+    batch = LadderBatch(XYModel(J=1.0), [(L, temps)], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
+                        proposal="gaussian", sigma0=1.0, initial_states=[initial_angles(seed)])
+    batch.autotune()
+    # Warm-up: thermalise and tune the proposal widths (adaptation stops here).
+    batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=True)
+    sigma = batch.sigma_t.copy_to_host()
+    n_slots = (args.steps + 2) * SWEEPS_PER_STEP // SAMPLE_INTERVAL
+    batch.allocate_samples(batch.sweeps + SAMPLE_INTERVAL, SAMPLE_INTERVAL, n_slots)
+    batch.run(SWEEPS_PER_STEP)  # captures the replay graphs outside the timed region
+    torch.cuda.synchronize()
+
+    # L2 flush buffer (larger than the 129 MB L2), written between timed steps.
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    updates_per_step = N_TEMPS * L * L * SWEEPS_PER_STEP
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    step_ms = []
+    barrier()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.run(SWEEPS_PER_STEP)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    total_ms = float(np.sum(step_ms))
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * updates_per_step * args.steps / (total_ms * 1e6)
+
+    # Dominant kernel: the window kernel, timed alone on the same stream.
+    from mcgb import _lib
+    import ctypes
+    w = batch._window(EXCHANGE_INTERVAL)
+    _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+    torch.cuda.synchronize()
+    reps = 20
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for _ in range(reps):
+        _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+    k1.record(stream)
+    torch.cuda.synchronize()
+    window_ms = k0.elapsed_time(k1) / reps
+    alg_bytes = BYTES_PER_UPDATE * N_TEMPS * L * L * EXCHANGE_INTERVAL
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (window_ms * 1e-3) / 1e9
+
+    # End to end through the public API with host buffers: every step uploads
+    # the ladder's angles and RNG streams from pinned memory, runs 100 sweeps
+    # and reads back the angles, RNG streams and the step's samples.
+    host = batch.pinned_state_buffers()
+    out = batch.pinned_state_buffers()
+    n_s = SWEEPS_PER_STEP // SAMPLE_INTERVAL
+    batch.download_state(host)
+    torch.cuda.synchronize()
+    batch.allocate_samples(batch.sweeps + SAMPLE_INTERVAL, SAMPLE_INTERVAL, n_s)
+    out_samples = torch.empty(batch.samples.nbytes, dtype=torch.uint8, pin_memory=True)
+    e2e_ms = []
+    for i in range(args.steps + 1):  # the first iteration captures graphs, untimed
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.upload_state(host)
+        batch.run(SWEEPS_PER_STEP)
+        batch.download_state(out)
+        out_samples.copy_(batch.samples.raw(), non_blocking=True)
+        e1.record(stream)
+        e1.synchronize()
+        if i > 0:
+            e2e_ms.append(e0.elapsed_time(e1))
+    h2d = sum(t.numel() for t in host.values())
+    d2h = sum(t.numel() for t in out.values()) + out_samples.numel()
+    e2e_total = float(np.sum(e2e_ms))
+    if dist is not None:
+        t = torch.tensor([e2e_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * updates_per_step * args.steps / (e2e_total * 1e6)
+
+    # Plain FP64 form on the same ladder (one lattice per launch), bounded.
+    plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
+    launches = args.steps * (SWEEPS_PER_STEP // EXCHANGE_INTERVAL) * 3
+
+    line = None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "updates/ns", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded uniform angles, reference has no dataset)",
+            "config": {"workload": WORKLOAD, "L": L, "replicas_per_gpu": N_TEMPS,
+                       "sweeps_per_step": SWEEPS_PER_STEP, "exchange_interval": EXCHANGE_INTERVAL,
+                       "sample_interval": SAMPLE_INTERVAL, "cluster_size": batch.cluster_size,
+                       "threads": batch.threads, "l2": "flushed (256 MB write) between timed steps",
+                       "parallelism": f"independent ladders x{world}"},
+            "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "window_kernel<XYPolicy>", "kernel_ms": window_ms,
+                         "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind},
+            "clocks": clk,
+            "gpu_launches": launches,
+            "tuned_sigma_range": [float(sigma.min()), float(sigma.max())],
+        }
+        if plain is not None:
+            line["plain_fp64"] = {"value": plain, "unit": "updates/ns",
+                                  "form": "one lattice per launch, float64 state and arithmetic"}
+            line["speedup_vs_plain_fp64"] = value / plain
+    return line
+
+
+def plain_fp64_rate(batch, sigma, seed):
+    """The plain form: every replica in its own launches (4 colours), float64
+    angles, float64 Gaussian proposals and exponentials; the exchange energies
+    from a float64 reduction per lattice.  Times 20 sweeps with 2 exchanges."""
+    import torch
+
+    from mcgb import _lib, device
+    from mcgb.rng import create_xoroshiro128p_states
+
+    R = N_TEMPS
+    theta = device.to_device(initial_angles(seed).astype(np.float64))
+    rng = create_xoroshiro128p_states(R * L * L, seed)
+    betas64 = device.to_device(1.0 / temperatures())
+    betas32 = device.to_device((1.0 / temperatures()).astype(np.float32))
+    sig = device.to_device(sigma.astype(np.float64))
+    energies = device.device_zeros(R, np.float64)
+    w2t = device.to_device(np.arange(R, dtype=np.int32))
+    t2w = device.to_device(np.arange(R, dtype=np.int32))
+    prng = create_xoroshiro128p_states(R - 1, seed + 1)
+    counts = device.device_zeros((3, R - 1), np.int64)
+    trips = device.to_device(np.zeros((5, R), np.int64))
+    s = _lib.stream_handle()
+
+    def sweeps(n, start):
+        for k in range(n):
+            for r in range(R):
+                for c in range(4):
+                    _lib.call("mcgb_xy64_update_color", theta.cptr, rng.cptr, betas64.cptr, sig.cptr, R, L, r, c,
+                              1.0, 1.5, s)
+            if (start + k + 1) % EXCHANGE_INTERVAL == 0:
+                for r in range(R):
+                    _lib.call("mcgb_xy64_energy", theta.cptr, R, L, r, 1.0, energies.cptr, s)
+                _lib.call("mcgb_pt_exchange", energies.cptr, betas32.cptr, w2t.cptr, t2w.cptr, prng.cptr,
+                          counts.cptr, trips.cptr, R, ((start + k) // EXCHANGE_INTERVAL) & 1, start + k + 1, s)
+
+    sweeps(2, 0)
+    torch.cuda.synchronize()
+    n = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sweeps(n, 2)
+    e1.record()
+    torch.cuda.synchronize()
+    return R * L * L * n / (e0.elapsed_time(e1) * 1e6)
+
+
+def profile_windows(cluster_size=4, threads=1024):
+    """Small fixed case for ncu: the bench ladder, 3 warm windows + 3 windows."""
+    import ctypes
+
+    import torch
+
+    from mcgb import _lib
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+
+    seed = 42 + L
+    b = LadderBatch(XYModel(J=1.0), [(L, temperatures())], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
+                    proposal="gaussian", sigma0=0.93, cluster_size=cluster_size, threads=threads,
+                    initial_states=[initial_angles(seed)])
+    w = b._window(EXCHANGE_INTERVAL)
+    for _ in range(6):
+        _lib.call("mcgb_batch_window_run", b.model_id, ctypes.byref(w), _lib.stream_handle())
+    torch.cuda.synchronize()
+    print("profile windows done")
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["mcgb", "reference"], default="mcgb")
+    ap.add_argument("--skip-plain", action="store_true", help="do not time the plain FP64 form")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling driver: set up the ladder, then launch 6 window kernels and exit")
+    ap.add_argument("--profile-shape", default="4,1024", help="cluster_size,threads for --profile")
+    args = ap.parse_args()
+    if args.profile:
+        c, t = (int(x) for x in args.profile_shape.split(","))
+        profile_windows(c, t)
+        return
+    if args.warmup < 3:
+        ap.error("warm-up must be at least 3 steps")
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_mcgb(args, rank, world)
+        if line is not None and not args.no_cpu_baseline:
+            cores = os.cpu_count() or 1
+            v, dt = cpu_sample(cores, 500)
+            line["cpu_baseline"] = {"value": v, "unit": "updates/ns", "cores": cores, "kind": "port",
+                                    "sample": f"500 sweeps of the same ladder with 50 exchanges, {cores} OpenMP "
+                                              f"threads, {dt:.1f} s (the reference has no CPU sweep; its kernels "
+                                              f"restated in C)"}
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

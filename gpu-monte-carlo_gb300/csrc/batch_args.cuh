@@ -54,9 +54,9 @@ inline BatchArgs make_args(const mcgb_batch_window &w)
     return a;
 }
 
-// Largest plaquette count a CTA holds, after validating the table against
-// the cluster shape.  Returns a negative status on error.
-inline long long validate_window(const mcgb_batch_window &w)
+// Largest L of the batch, after validating the table against the cluster
+// shape.  Returns a negative status on error.
+inline int validate_window(const mcgb_batch_window &w)
 {
     MCGB_REQUIRE(w.table && w.host_table && w.work_ptr && w.work_idx, "batch window: null table/work list");
     MCGB_REQUIRE(w.state && w.rng && w.betas && w.w2t && w.e_run && w.energies && w.accepted && w.clock,
@@ -68,7 +68,7 @@ inline long long validate_window(const mcgb_batch_window &w)
     MCGB_REQUIRE(w.n_sweeps >= 0, "batch window: n_sweeps must be >= 0");
     MCGB_REQUIRE(w.samples == nullptr || (w.n_slots >= 1 && w.n_temps_total >= 1 && w.sample_interval >= 1),
                  "batch window: bad sample buffer");
-    long long max_npl = 0;
+    int max_L = 0;
     for (int r = 0; r < w.n_replicas; ++r) {
         const mcgb_replica &rep = w.host_table[r];
         MCGB_REQUIRE(rep.L >= 4 && rep.L % (2 * w.cluster_size) == 0,
@@ -78,20 +78,20 @@ inline long long validate_window(const mcgb_batch_window &w)
                          rep.ladder_start <= r && r < rep.ladder_start + rep.n_temps,
                      "batch window: replica %d has an inconsistent ladder range", r);
         MCGB_REQUIRE(rep.state_offset >= 0, "batch window: negative state offset");
-        const long long npl = (long long)rep.L * rep.L / (4 * w.cluster_size);
-        if (npl > max_npl) max_npl = npl;
+        if (rep.L > max_L) max_L = rep.L;
     }
     MCGB_REQUIRE(w.samples == nullptr || w.n_temps_total >= w.n_replicas,
                  "batch window: n_temps_total must cover every replica");
-    return max_npl;
+    return max_L;
 }
 
 template <class M, int NPMAX>
-int launch_window(const BatchArgs &a, const mcgb_batch_window &w, long long max_npl, cudaStream_t stream,
+int launch_window(const BatchArgs &a, const mcgb_batch_window &w, int max_L, cudaStream_t stream,
                   const char *name)
 {
     auto kern = window_kernel<M, NPMAX>;
-    const size_t smem = window_smem_bytes<M>((int)max_npl);
+    const size_t smem =
+        window_smem_bytes<M>((long long)max_L * max_L / (4 * w.cluster_size), (long long)max_L / 2);
     MCGB_REQUIRE(smem <= 232448, "%s: a strip needs %zu bytes of shared memory (> 227 KB); use a larger "
                                  "cluster_size", name, smem);
     int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),

@@ -19,8 +19,8 @@
 //   c=1: up (3,-1,0)  down (3,0,0)  left (0,0,0)  right (0,0,+1)
 //   c=2: up (0,0,0)   down (0,+1,0) left (3,0,-1) right (3,0,0)
 //   c=3: up (1,0,0)   down (1,+1,0) left (2,0,0)  right (2,0,+1)
-// Columns wrap within the strip (strips are whole rows); a row offset that
-// leaves the strip reads the neighbouring CTA's shared memory (DSMEM).
+// Columns wrap within the strip (strips are whole rows); rows outside the
+// strip are halo rows kept up to date by the neighbouring CTAs.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -31,77 +31,10 @@ namespace mcgb {
 
 namespace cg = cooperative_groups;
 
-// Plane and plaquette offsets of the four nearest neighbours (up, down, left, right).
+// Plane and plaquette-row/column offsets of a neighbour.
 struct NbrSpec {
     int plane, dpr, dpc;
 };
-
-__device__ __forceinline__ NbrSpec nbr_up(int c)
-{
-    return c < 2 ? NbrSpec{c + 2, -1, 0} : NbrSpec{c - 2, 0, 0};
-}
-__device__ __forceinline__ NbrSpec nbr_down(int c)
-{
-    return c < 2 ? NbrSpec{c + 2, 0, 0} : NbrSpec{c - 2, 1, 0};
-}
-__device__ __forceinline__ NbrSpec nbr_left(int c)
-{
-    return (c & 1) ? NbrSpec{c - 1, 0, 0} : NbrSpec{c + 1, 0, -1};
-}
-__device__ __forceinline__ NbrSpec nbr_right(int c)
-{
-    return (c & 1) ? NbrSpec{c - 1, 0, 1} : NbrSpec{c + 1, 0, 0};
-}
-// Diagonal neighbours used by the He3 gradient cells: (i-1, j+1), (i+1, j-1).
-__device__ __forceinline__ NbrSpec nbr_upright(int c)
-{
-    switch (c) {
-    case 0: return NbrSpec{3, -1, 0};
-    case 1: return NbrSpec{2, -1, 1};
-    case 2: return NbrSpec{1, 0, 0};
-    default: return NbrSpec{0, 0, 1};
-    }
-}
-__device__ __forceinline__ NbrSpec nbr_downleft(int c)
-{
-    switch (c) {
-    case 0: return NbrSpec{3, 0, -1};
-    case 1: return NbrSpec{2, 0, 0};
-    case 2: return NbrSpec{1, 1, -1};
-    default: return NbrSpec{0, 1, 0};
-    }
-}
-
-// Geometry of the strip a CTA holds.
-struct Strip {
-    int L;     // lattice size
-    int LP;    // plaquettes per row = L/2
-    int HP;    // plaquette rows in this CTA = L/(2C)
-    int NPL;   // plaquettes in this CTA = HP*LP
-    int rank;  // CTA rank in the cluster
-    int C;     // cluster size
-};
-
-// Pointer to the element of `planes` (local shared memory, 4 planes of NPL)
-// that neighbour `s` of plaquette (pr, pc) refers to; rows outside the strip
-// map to the neighbouring CTA of the cluster.
-template <typename T>
-__device__ __forceinline__ T *nbr_ptr(T *planes, const Strip &g, NbrSpec s, int pr, int pc)
-{
-    int r = pr + s.dpr;
-    int c = pc + s.dpc;
-    c = c < 0 ? c + g.LP : (c >= g.LP ? c - g.LP : c);
-    T *local = planes + s.plane * g.NPL;
-    if (r < 0) {
-        const int up = g.rank == 0 ? g.C - 1 : g.rank - 1;
-        return static_cast<T *>(__cluster_map_shared_rank(local + (g.HP - 1) * g.LP + c, up));
-    }
-    if (r >= g.HP) {
-        const int dn = g.rank + 1 == g.C ? 0 : g.rank + 1;
-        return static_cast<T *>(__cluster_map_shared_rank(local + c, dn));
-    }
-    return local + r * g.LP + c;
-}
 
 // Knuth TwoSum: s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
@@ -121,14 +54,15 @@ __device__ __forceinline__ void comp_add(float &sum, float &comp, float x)
 }
 
 // The slot of the sample taken after sweep `sweep_no` (1-based, cumulative),
-// or -1 when no sample is due or the buffer is full.
+// or -1 when no sample is due.  The buffer is a ring of n_slots samples: a
+// run longer than the buffer overwrites the oldest slots, so a replayed graph
+// can keep writing into a fixed buffer that the host drains.
 __device__ __forceinline__ int sample_slot(long long sweep_no, long long first, int interval, int n_slots)
 {
-    if (interval <= 0 || sweep_no < first) return -1;
+    if (interval <= 0 || n_slots <= 0 || sweep_no < first) return -1;
     const long long d = sweep_no - first;
     if (d % interval) return -1;
-    const long long slot = d / interval;
-    return slot < n_slots ? (int)slot : -1;
+    return (int)((d / interval) % n_slots);
 }
 
 // Block-wide double sums of NC values into `out` (thread 0 valid); scratch

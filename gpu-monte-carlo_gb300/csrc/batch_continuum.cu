@@ -9,7 +9,7 @@ int continuum_window(int model, const mcgb_batch_window &, cudaStream_t)
     return MCGB_EINVAL;
 }
 
-int continuum_smem(int model, long long)
+int64_t continuum_smem(int model, int, int)
 {
     set_error("batched engine: model %d is not available yet", model);
     return MCGB_EINVAL;

@@ -3,16 +3,18 @@
 // Ising (models/ising/update.py:7-29): int8 spins in shared memory, one RNG
 // draw per visit, acceptance `dE <= 0 or u < expf(-beta*dE)` with the five
 // possible expf values per replica evaluated once per window with the same
-// float32 expf -- bit-identical to the per-colour kernel.  The window's final
-// energy is the exact integer bond count times J.
+// float32 expf and turned into exact integer thresholds on the raw draw --
+// bit-identical to the per-colour kernel.  The window's final energy is the
+// exact integer bond count times J.
 //
 // XY (models/xy/update.py:6-54 and the Gaussian variant): shared memory
 // holds (cos, sin) of every angle, so an update evaluates one sincos of the
 // proposal instead of eight cosines:
 //   dE = -J [ (cos t' - cos t) S_c + (sin t' - sin t) S_s ],
 // S_c, S_s the sums over the four neighbours' cached (cos, sin).  Proposal,
-// Box-Muller and acceptance use the fast float32 intrinsics; the draw
-// sequence per visit is the oracle's (uniform: u, v; Gaussian: u1, u2, v).
+// Box-Muller and acceptance use the fast float32 intrinsics and 23-bit
+// uniforms; the draw sequence per visit is the oracle's (uniform: u, v;
+// Gaussian: u1, u2, v), so the streams stay in step with it.
 // Accepted changes accumulate per thread with compensation and update the
 // replica's running energy; samples read it instead of re-summing bonds.
 #include "batch_args.cuh"
@@ -30,9 +32,15 @@ struct IsingPolicy {
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
 
+    // u < expf(-beta*dE) for the float32 uniform u of draw x is
+    // (x >> 11) < M, with M the integer threshold of that float (exact, see
+    // mcgb_unit_threshold); k = 2*s*sum in {-8, -4, 0, 4, 8}.
     struct Ctx {
-        float t[5];  // acceptance thresholds for k = -8, -4, 0, 4, 8
+        unsigned long long m[5];
         float J;
+    };
+    struct Prop {
+        unsigned long long m;  // x >> 11 of the visit's draw
     };
 
     static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
@@ -43,8 +51,8 @@ struct IsingPolicy {
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
             const float dE = (float)(4 * q - 8) * a.J;
-            // u <= 1 < 2 accepts every move with dE <= 0.
-            x.t[q] = dE <= 0.0f ? 2.0f : expf(-beta * dE);
+            // dE <= 0 accepts every draw: u <= 1 < 2.
+            x.m[q] = mcgb_unit_threshold(dE <= 0.0f ? 2.0f : expf(-beta * dE));
         }
         return x;
     }
@@ -57,21 +65,26 @@ struct IsingPolicy {
         static_cast<int8_t *>(a.state)[site] = cell;
     }
     template <int C_>
-    static __device__ __forceinline__ bool update(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *,
-                                                  ulonglong2 &st, float &dE)
+    static __device__ __forceinline__ Prop propose(const Ctx &, const Cell &, const float *, ulonglong2 &st)
+    {
+        return Prop{(unsigned long long)(xoro_next(st) >> 11)};
+    }
+    template <int C_>
+    static __device__ __forceinline__ bool decide(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *,
+                                                  const Prop &pr, float &dE)
     {
         const int s = me;
-        const int sum = nb.at(nbr_up(C_)) + nb.at(nbr_down(C_)) + nb.at(nbr_left(C_)) + nb.at(nbr_right(C_));
+        const int sum = MCGB_NBR(nb, kUp(C_)) + MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kLeft(C_)) +
+                        MCGB_NBR(nb, kRight(C_));
         const int k = 2 * s * sum;
-        const float u = xoro_uniform_f32(st);
         dE = (float)k * x.J;
         // Static indices keep the five thresholds in registers.
-        float t = x.t[0];
-        t = k == -4 ? x.t[1] : t;
-        t = k == 0 ? x.t[2] : t;
-        t = k == 4 ? x.t[3] : t;
-        t = k == 8 ? x.t[4] : t;
-        if (u < t) {
+        unsigned long long t = x.m[0];
+        t = k == -4 ? x.m[1] : t;
+        t = k == 0 ? x.m[2] : t;
+        t = k == 4 ? x.m[3] : t;
+        t = k == 8 ? x.m[4] : t;
+        if (pr.m < t) {
             me = (int8_t)(-s);
             return true;
         }
@@ -82,14 +95,14 @@ struct IsingPolicy {
                                                    const float *, double *v)
     {
         const int s = me;
-        v[0] += (double)(s * (nb.at(nbr_down(C_)) + nb.at(nbr_right(C_))));
+        v[0] += (double)(s * (MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kRight(C_))));
         v[1] += (double)s;
     }
     template <int C_>
     static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
                                                        const float *, double &e)
     {
-        e += (double)(me * (nb.at(nbr_down(C_)) + nb.at(nbr_right(C_))));
+        e += (double)(me * (MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kRight(C_))));
     }
     static __device__ __forceinline__ void finish_sample(const Ctx &x, double *v) { v[0] *= -(double)x.J; }
     static __device__ __forceinline__ double finish_energy(const Ctx &x, double bonds) { return -(double)x.J * bonds; }
@@ -109,6 +122,10 @@ struct XYPolicy {
     struct Ctx {
         float beta, sigma, J, delta;
         bool gauss;
+    };
+    // Proposal angle, its (cos, sin) and the acceptance uniform.
+    struct Prop {
+        float tp, cp, sp, v;
     };
 
     static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
@@ -133,40 +150,49 @@ struct XYPolicy {
         static_cast<float *>(a.state)[site] = own[0];
         a.aux[site] = cell;
     }
+    // Draws (in order): Gaussian u1, u2, accept v; uniform u, accept v.  The
+    // mixed form uses 23-bit uniforms (mcgb_fast_unit).
     template <int C_>
-    static __device__ __forceinline__ bool update(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *own,
-                                                  ulonglong2 &st, float &dE)
+    static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &, const float *own, ulonglong2 &st)
     {
         const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
-        const float2 a = nb.at(nbr_up(C_)), b = nb.at(nbr_down(C_));
-        const float2 c = nb.at(nbr_left(C_)), d = nb.at(nbr_right(C_));
-        const float sc = (a.x + b.x) + (c.x + d.x);
-        const float ss = (a.y + b.y) + (c.y + d.y);
         const float t = own[0];
-        float tp;
+        Prop q;
         if (x.gauss) {
-            float u1 = xoro_uniform_f32(st);
-            const float u2 = xoro_uniform_f32(st);
+            float u1 = mcgb_fast_unit(xoro_next(st));
+            const float u2 = mcgb_fast_unit(xoro_next(st));
             if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
+            const float t2 = -2.0f * __logf(u1);
             // cos(2 pi u2) = -cos(2 pi u2 - pi), evaluated on [-pi, pi].
-            const float z = -sqrtf(-2.0f * __logf(u1)) * __cosf(fmaf(two_pi, u2, -pi));
-            tp = fmaf(x.sigma, z, t);
+            const float z = -(t2 * rsqrtf(t2)) * __cosf(fmaf(two_pi, u2, -pi));
+            float tp = fmaf(x.sigma, z, t);
             tp -= two_pi * floorf((tp + pi) * (1.0f / two_pi));
             if (tp >= pi) tp -= two_pi;
             if (tp < -pi) tp += two_pi;
+            q.tp = tp;
         } else {
-            const float u = xoro_uniform_f32(st);
-            tp = t + x.delta * (2.0f * u - 1.0f);
+            const float u = mcgb_fast_unit(xoro_next(st));
+            float tp = t + x.delta * (2.0f * u - 1.0f);
             if (tp >= pi) tp -= two_pi;
             else if (tp < -pi) tp += two_pi;
+            q.tp = tp;
         }
-        float sp, cp;
-        __sincosf(tp, &sp, &cp);
-        dE = -x.J * ((cp - me.x) * sc + (sp - me.y) * ss);
-        const float v = xoro_uniform_f32(st);
-        if (dE <= 0.0f || v < __expf(-x.beta * dE)) {
-            own[0] = tp;
-            me = make_float2(cp, sp);
+        __sincosf(q.tp, &q.sp, &q.cp);
+        q.v = mcgb_fast_unit(xoro_next(st));
+        return q;
+    }
+    template <int C_>
+    static __device__ __forceinline__ bool decide(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *own,
+                                                  const Prop &q, float &dE)
+    {
+        const float2 a = MCGB_NBR(nb, kUp(C_)), b = MCGB_NBR(nb, kDown(C_));
+        const float2 c = MCGB_NBR(nb, kLeft(C_)), d = MCGB_NBR(nb, kRight(C_));
+        const float sc = (a.x + b.x) + (c.x + d.x);
+        const float ss = (a.y + b.y) + (c.y + d.y);
+        dE = -x.J * ((q.cp - me.x) * sc + (q.sp - me.y) * ss);
+        if (dE <= 0.0f || q.v < __expf(-x.beta * dE)) {
+            own[0] = q.tp;
+            me = make_float2(q.cp, q.sp);
             return true;
         }
         return false;
@@ -175,7 +201,7 @@ struct XYPolicy {
     static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
                                                    const float *, double *v)
     {
-        const float2 dn = nb.at(nbr_down(C_));
+        const float2 dn = MCGB_NBR(nb, kDown(C_));
         v[1] += me.x;
         v[2] += me.y;
         v[3] += me.x * dn.x + me.y * dn.y;
@@ -254,20 +280,21 @@ int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s)
 int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s)
 {
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w.aux != nullptr, "XY window: null (cos, sin) cache");
-    const long long max_npl = validate_window(w);
-    if (max_npl < 0) return (int)max_npl;
+    const int max_L = validate_window(w);
+    if (max_L < 0) return max_L;
     const BatchArgs a = make_args(w);
     if (model == MCGB_MODEL_ISING)
-        return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, max_npl, s, "ising window")
-                               : launch_window<IsingPolicy, 2>(a, w, max_npl, s, "ising window");
-    return w.threads > 512 ? launch_window<XYPolicy, 1>(a, w, max_npl, s, "xy window")
-                           : launch_window<XYPolicy, 2>(a, w, max_npl, s, "xy window");
+        return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, max_L, s, "ising window")
+                               : launch_window<IsingPolicy, 2>(a, w, max_L, s, "ising window");
+    return w.threads > 512 ? launch_window<XYPolicy, 1>(a, w, max_L, s, "xy window")
+                           : launch_window<XYPolicy, 2>(a, w, max_L, s, "xy window");
 }
 
-int lattice_smem(int model, long long max_npl)
+int64_t lattice_smem(int model, int max_L, int C)
 {
-    return (int)(model == MCGB_MODEL_ISING ? window_smem_bytes<IsingPolicy>((int)max_npl)
-                                           : window_smem_bytes<XYPolicy>((int)max_npl));
+    const long long npl = (long long)max_L * max_L / (4 * C), lp = max_L / 2;
+    return (int64_t)(model == MCGB_MODEL_ISING ? window_smem_bytes<IsingPolicy>(npl, lp)
+                                               : window_smem_bytes<XYPolicy>(npl, lp));
 }
 
 int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out)

@@ -5,12 +5,12 @@
 namespace mcgb {
 
 int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s);
-int lattice_smem(int model, long long max_npl);
+int64_t lattice_smem(int model, int max_L, int C);
 int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out);
 int lattice_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s);
 int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s);
 int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s);
-int continuum_smem(int model, long long max_npl);
+int64_t continuum_smem(int model, int max_L, int C);
 int continuum_max_clusters(int model, int C, int threads, size_t smem, int *out);
 int continuum_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s);
 
@@ -162,11 +162,12 @@ extern "C" int mcgb_batch_channels(int model)
     }
 }
 
-extern "C" int64_t mcgb_batch_smem_bytes(int model, int64_t max_plaquettes)
+extern "C" int64_t mcgb_batch_smem_bytes(int model, int max_L, int cluster_size)
 {
     MCGB_REQUIRE(known_model(model), "unknown model %d", model);
-    MCGB_REQUIRE(max_plaquettes >= 1, "max_plaquettes must be >= 1");
-    return is_lattice(model) ? lattice_smem(model, max_plaquettes) : continuum_smem(model, max_plaquettes);
+    MCGB_REQUIRE(cluster_size >= 1 && cluster_size <= 16, "cluster_size must be 1..16");
+    MCGB_REQUIRE(max_L >= 4 && max_L % (2 * cluster_size) == 0, "max_L must be a multiple of 2 * cluster_size");
+    return is_lattice(model) ? lattice_smem(model, max_L, cluster_size) : continuum_smem(model, max_L, cluster_size);
 }
 
 extern "C" int mcgb_batch_max_clusters(int model, int cluster_size, int threads, int64_t smem_bytes, int *out)

@@ -11,16 +11,34 @@
 // launches, since every site draws from its own stream.  Models whose sites
 // couple colours 1 and 2 (He3's diagonal gradient cells) set kSplitMiddle and
 // get a barrier between them.  Samples due inside the window are reduced
-// over the cluster and written in temperature order.  At the end the
-// accepted energy changes update the replica's compensated running energy.
+// over the cluster and written in temperature order.
+//
+// Halo rows.  Each colour plane of a strip is stored with one halo row above
+// and one below, so every neighbour read is a local shared-memory load at a
+// compile-time offset.  Only two halos are ever read: planes 2 and 3 (odd
+// rows) are read one plaquette row above the strip, planes 0 and 1 (even
+// rows) one row below.  When a thread accepts a move on its strip's last
+// plaquette row of plane 2/3 it also stores the new cell into the top halo of
+// the CTA below (DSMEM store); on the first row of plane 0/1, into the bottom
+// halo of the CTA above.  The cluster barrier that ends the phase publishes
+// those stores.  With C = 1 the neighbour CTA is the CTA itself.
+//
+// Pipelining across barriers.  An update is split into propose<c> (every
+// random draw of the visit, in the reference's draw order, and whatever
+// depends only on the site's own value) and decide<c> (neighbour reads,
+// energy change, acceptance).  The cluster barrier is split into arrive and
+// wait: a thread arrives after deciding a colour, proposes its next colour's
+// moves, then waits, so the barrier latency hides behind independent work.
 //
 // Policy M supplies: Args (with the common fields below), Cell (the
 // per-site shared-memory record neighbours read), kOwnFloats (extra
-// per-site floats only the owner reads), kChannels, kSplitMiddle, and
+// per-site floats only the owner reads), kChannels, kSplitMiddle, Prop (the
+// per-visit proposal), and
 //   Ctx  prepare(const Args&, int r, const mcgb_replica&)
 //   void load(const Args&, int64_t site, Cell&, float* own)
 //   void store(const Args&, int64_t site, const Cell&, const float* own)
-//   bool update<c>(const Ctx&, Nbrs, Cell&, float* own, ulonglong2&, float& dE)
+//   Prop propose<c>(const Ctx&, const Cell&, const float* own, ulonglong2&)
+//   bool decide<c>(const Ctx&, Nbrs, Cell&, float* own, const Prop&, float& dE)
 //   void measure<c>(const Ctx&, Nbrs, const Cell&, const float* own, double* v)
 //   void finish_sample(const Ctx&, double* v)  (channel 0 holds the energy)
 // and two flags: kEnergyFromDelta (channel 0 = running energy + accepted
@@ -33,15 +51,58 @@
 
 namespace mcgb {
 
-// Neighbour accessor handed to the policies.
+// Compile-time neighbour specs (plane, dpr, dpc) of colour c.
+__host__ __device__ constexpr NbrSpec kUp(int c) { return c < 2 ? NbrSpec{c + 2, -1, 0} : NbrSpec{c - 2, 0, 0}; }
+__host__ __device__ constexpr NbrSpec kDown(int c) { return c < 2 ? NbrSpec{c + 2, 0, 0} : NbrSpec{c - 2, 1, 0}; }
+__host__ __device__ constexpr NbrSpec kLeft(int c) { return (c & 1) ? NbrSpec{c - 1, 0, 0} : NbrSpec{c + 1, 0, -1}; }
+__host__ __device__ constexpr NbrSpec kRight(int c) { return (c & 1) ? NbrSpec{c - 1, 0, 1} : NbrSpec{c + 1, 0, 0}; }
+__host__ __device__ constexpr NbrSpec kUpRight(int c)
+{
+    return c == 0 ? NbrSpec{3, -1, 0} : c == 1 ? NbrSpec{2, -1, 1} : c == 2 ? NbrSpec{1, 0, 0} : NbrSpec{0, 0, 1};
+}
+__host__ __device__ constexpr NbrSpec kDownLeft(int c)
+{
+    return c == 0 ? NbrSpec{3, 0, -1} : c == 1 ? NbrSpec{2, 0, 0} : c == 2 ? NbrSpec{1, 1, -1} : NbrSpec{0, 1, 0};
+}
+
+// A thread's plaquette in the haloed strip: own row offset o = (pr + 1) * LP,
+// rows above/below om/op, column pc and its periodic neighbours pcm/pcp.
+struct Site {
+    int o, om, op, pc, pcm, pcp;
+    int pr;
+};
+
+__device__ __forceinline__ Site make_site(int p, int LP)
+{
+    Site s;
+    s.pr = p / LP;
+    s.pc = p - s.pr * LP;
+    s.o = (s.pr + 1) * LP;
+    s.om = s.o - LP;
+    s.op = s.o + LP;
+    s.pcm = s.pc == 0 ? LP - 1 : s.pc - 1;
+    s.pcp = s.pc + 1 == LP ? 0 : s.pc + 1;
+    return s;
+}
+
+// Neighbour accessor handed to the policies: every read is local.
 template <typename Cell>
 struct Nbrs {
-    Cell *planes;
-    Strip g;
-    int pr, pc;
+    const Cell *planes;
+    int PS;  // plane stride (HP + 2) * LP
+    Site s;
 
-    __device__ __forceinline__ const Cell &at(NbrSpec s) const { return *nbr_ptr(planes, g, s, pr, pc); }
+    template <int P, int DR, int DC>
+    __device__ __forceinline__ const Cell &get() const
+    {
+        const int row = DR < 0 ? s.om : (DR > 0 ? s.op : s.o);
+        const int col = DC < 0 ? s.pcm : (DC > 0 ? s.pcp : s.pc);
+        return planes[P * PS + row + col];
+    }
 };
+
+// The neighbour of `nb` described by the constexpr NbrSpec `spec`.
+#define MCGB_NBR(nb, spec) ((nb).template get<(spec).plane, (spec).dpr, (spec).dpc>())
 
 struct WindowCommon {
     const mcgb_replica *table;
@@ -53,7 +114,7 @@ struct WindowCommon {
     float *e_run;          // 2 per replica: compensated running energy (hi, lo)
     double *energies;      // out: per replica, hi + lo after the window
     long long *accepted;   // per replica, += accepted moves
-    double *samples;       // [n_slots][kChannels][n_temps_total] or null
+    double *samples;       // ring [n_slots][kChannels][n_temps_total] or null
     double *staging;       // [kChannels][n_replicas]: window-end sample, walker order
     int n_temps_total;
     int n_slots;
@@ -65,75 +126,133 @@ struct WindowCommon {
 
 constexpr int kRedDoubles = 16;  // per-CTA cluster reduction slots
 
+// Shared memory of a strip with npl plaquettes in rows of lp.
 template <class M>
-__host__ __device__ constexpr size_t cell_bytes()
+__host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp)
 {
-    return sizeof(typename M::Cell) + sizeof(float) * M::kOwnFloats;
+    return sizeof(double) * (kRedDoubles + 32 * (M::kChannels + 3)) +
+           (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
+           (size_t)4 * npl * sizeof(float) * M::kOwnFloats;
 }
 
-template <class M>
-__host__ __device__ inline size_t window_smem_bytes(int max_npl)
-{
-    return sizeof(double) * (kRedDoubles + 32 * (M::kChannels + 2)) + (size_t)4 * max_npl * cell_bytes<M>();
-}
+struct StripCtx {
+    int LP, HP, NPL, PS, up, dn;
+};
 
-template <class M, int NPMAX, int C_>
-__device__ __forceinline__ void colour_pass(const typename M::Args &a, const typename M::Ctx &ctx,
-                                            cg::cluster_group &cluster, typename M::Cell *cells,
-                                            float *own, const Strip &g, ulonglong2 (&st)[NPMAX > 0 ? NPMAX : 1][4],
-                                            bool regs, int64_t base, int64_t gplane, float &dsum,
-                                            float &dcomp, int &nacc)
+// After an accepted move on a boundary plaquette, copy the new cell into the
+// halo of the neighbouring CTA that reads it.
+template <int C_, typename Cell>
+__device__ __forceinline__ void push_halo(Cell *cells, const StripCtx &g, const Site &s, const Cell &v)
 {
-    const int T = blockDim.x;
-    ulonglong2 *rng_g = static_cast<ulonglong2 *>(a.c.rng);
-    if (regs) {
-#pragma unroll
-        for (int k = 0; k < NPMAX; ++k) {
-            const int p = threadIdx.x + k * T;
-            if (p < g.NPL) {
-                Nbrs<typename M::Cell> nb{cells, g, p / g.LP, p % g.LP};
-                float dE;
-                if (M::template update<C_>(ctx, nb, cells[C_ * g.NPL + p], own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats,
-                                           st[k][C_], dE)) {
-                    comp_add(dsum, dcomp, dE);
-                    ++nacc;
-                }
-            }
+    if (C_ < 2) {
+        if (s.pr == 0) {
+            Cell *dst = cells + C_ * g.PS + (g.HP + 1) * g.LP + s.pc;
+            *static_cast<Cell *>(__cluster_map_shared_rank(dst, g.up)) = v;
         }
     } else {
-        for (int p = threadIdx.x; p < g.NPL; p += T) {
-            const int64_t idx = base + C_ * gplane + p;
-            ulonglong2 s = rng_g[idx];
-            Nbrs<typename M::Cell> nb{cells, g, p / g.LP, p % g.LP};
+        if (s.pr == g.HP - 1) {
+            Cell *dst = cells + C_ * g.PS + s.pc;
+            *static_cast<Cell *>(__cluster_map_shared_rank(dst, g.dn)) = v;
+        }
+    }
+}
+
+// Split cluster barrier: arrive publishes this thread's shared-memory and
+// DSMEM stores (release); wait returns when every thread of the cluster has
+// arrived and makes their stores visible (acquire).  Calls must alternate.
+__device__ __forceinline__ void cluster_arrive()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait()
+{
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+template <class M, int NK, int C_>
+__device__ __forceinline__ void propose_pass(const typename M::Ctx &ctx, const typename M::Cell *cells,
+                                             const float *own, const StripCtx &g, const Site (&sites)[NK],
+                                             ulonglong2 (&st)[NK][4], typename M::Prop (&prop)[NK])
+{
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+        const int p = threadIdx.x + k * blockDim.x;
+        if (p < g.NPL)
+            prop[k] = M::template propose<C_>(ctx, cells[C_ * g.PS + sites[k].o + sites[k].pc],
+                                               own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, st[k][C_]);
+    }
+}
+
+template <class M, int NK, int C_>
+__device__ __forceinline__ void decide_pass(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
+                                            const StripCtx &g, const Site (&sites)[NK],
+                                            const typename M::Prop (&prop)[NK], float &dsum, float &dcomp,
+                                            int &nacc)
+{
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+        const int p = threadIdx.x + k * blockDim.x;
+        if (p < g.NPL) {
+            const Site &s = sites[k];
+            const Nbrs<typename M::Cell> nb{cells, g.PS, s};
+            typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
             float dE;
-            if (M::template update<C_>(ctx, nb, cells[C_ * g.NPL + p], own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats,
-                                       s, dE)) {
+            if (M::template decide<C_>(ctx, nb, me, own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, prop[k], dE)) {
                 comp_add(dsum, dcomp, dE);
                 ++nacc;
+                push_halo<C_>(cells, g, s, me);
             }
-            rng_g[idx] = s;
+        }
+    }
+}
+
+// Strips with more plaquettes than NK per thread keep their streams in
+// global memory and run propose + decide per plaquette, with full barriers.
+template <class M, int C_>
+__device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const typename M::Ctx &ctx,
+                                                typename M::Cell *cells, float *own, const StripCtx &g,
+                                                int64_t base, int64_t gplane, float &dsum, float &dcomp, int &nacc)
+{
+    ulonglong2 *rng_g = static_cast<ulonglong2 *>(a.c.rng);
+    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
+        const int64_t idx = base + C_ * gplane + p;
+        ulonglong2 sv = rng_g[idx];
+        const Site s = make_site(p, g.LP);
+        float *o = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
+        typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
+        const typename M::Prop pr = M::template propose<C_>(ctx, me, o, sv);
+        rng_g[idx] = sv;
+        const Nbrs<typename M::Cell> nb{cells, g.PS, s};
+        float dE;
+        if (M::template decide<C_>(ctx, nb, me, o, pr, dE)) {
+            comp_add(dsum, dcomp, dE);
+            ++nacc;
+            push_halo<C_>(cells, g, s, me);
         }
     }
 }
 
 template <class M, int C_>
-__device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, cg::cluster_group &cluster,
-                                               typename M::Cell *cells, float *own, const Strip &g,
-                                               double *v)
+__device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
+                                               const StripCtx &g, double *v)
 {
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
-        Nbrs<typename M::Cell> nb{cells, g, p / g.LP, p % g.LP};
-        M::template measure<C_>(ctx, nb, cells[C_ * g.NPL + p], own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, v);
+        const Site s = make_site(p, g.LP);
+        const Nbrs<typename M::Cell> nb{cells, g.PS, s};
+        M::template measure<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
+                                own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, v);
     }
 }
 
 template <class M, int C_>
-__device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, cg::cluster_group &cluster,
-                                              typename M::Cell *cells, float *own, const Strip &g, double &e)
+__device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
+                                              const StripCtx &g, double &e)
 {
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
-        Nbrs<typename M::Cell> nb{cells, g, p / g.LP, p % g.LP};
-        M::template energy_site<C_>(ctx, nb, cells[C_ * g.NPL + p], own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, e);
+        const Site s = make_site(p, g.LP);
+        const Nbrs<typename M::Cell> nb{cells, g.PS, s};
+        M::template energy_site<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
+                                    own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, e);
     }
 }
 
@@ -150,6 +269,7 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
 {
     using Cell = typename M::Cell;
     constexpr int NC = M::kChannels;
+    constexpr int NK = NPMAX > 0 ? NPMAX : 1;
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
@@ -157,39 +277,52 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
     const int T = blockDim.x, tid = threadIdx.x;
 
     extern __shared__ __align__(16) unsigned char smem[];
-    double *red = reinterpret_cast<double *>(smem);              // kRedDoubles
-    double *scratch = red + kRedDoubles;                           // 32 * (NC + 2)
-    unsigned char *tail = reinterpret_cast<unsigned char *>(scratch + 32 * (NC + 2));
+    double *red = reinterpret_cast<double *>(smem);  // kRedDoubles
+    double *scratch = red + kRedDoubles;               // 32 * (NC + 3)
+    Cell *cells = reinterpret_cast<Cell *>(scratch + 32 * (NC + 3));
 
     const WindowCommon &cm = a.c;
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
+    // DSMEM stores below need every CTA of the cluster to be running.
+    cluster.sync();
 
     for (int w = cm.work_ptr[cid]; w < cm.work_ptr[cid + 1]; ++w) {
         const int r = cm.work_idx[w];
         const mcgb_replica rep = cm.table[r];
-        Strip g;
-        g.L = rep.L;
+        StripCtx g;
         g.LP = rep.L >> 1;
         g.HP = rep.L / (2 * C);
         g.NPL = g.HP * g.LP;
-        g.rank = rank;
-        g.C = C;
-        Cell *cells = reinterpret_cast<Cell *>(tail);
-        float *own = reinterpret_cast<float *>(cells + 4 * g.NPL);
+        g.PS = (g.HP + 2) * g.LP;
+        g.up = rank == 0 ? C - 1 : rank - 1;
+        g.dn = rank + 1 == C ? 0 : rank + 1;
+        float *own = reinterpret_cast<float *>(
+            (reinterpret_cast<uintptr_t>(cells + 4 * g.PS) + 15) & ~static_cast<uintptr_t>(15));
         const int64_t gplane = (int64_t)g.LP * g.LP;
         const int64_t base = rep.state_offset + (int64_t)rank * g.NPL;
 
         const typename M::Ctx ctx = M::prepare(a, r, rep);
+        // Load the strip; boundary rows also go to the neighbours' halos.
         for (int c = 0; c < 4; ++c)
-            for (int p = tid; p < g.NPL; p += T)
-                M::load(a, base + c * gplane + p, cells[c * g.NPL + p], own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
+            for (int p = tid; p < g.NPL; p += T) {
+                const Site s = make_site(p, g.LP);
+                Cell &me = cells[c * g.PS + s.o + s.pc];
+                M::load(a, base + c * gplane + p, me, own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
+                if (c < 2 && s.pr == 0)
+                    *static_cast<Cell *>(
+                        __cluster_map_shared_rank(cells + c * g.PS + (g.HP + 1) * g.LP + s.pc, g.up)) = me;
+                if (c >= 2 && s.pr == g.HP - 1)
+                    *static_cast<Cell *>(__cluster_map_shared_rank(cells + c * g.PS + s.pc, g.dn)) = me;
+            }
 
         const bool regs = NPMAX > 0 && g.NPL <= NPMAX * T;
-        ulonglong2 st[NPMAX > 0 ? NPMAX : 1][4];
-        if (regs) {
+        ulonglong2 st[NK][4];
+        Site sites[NK];
 #pragma unroll
-            for (int k = 0; k < (NPMAX > 0 ? NPMAX : 1); ++k) {
-                const int p = tid + k * T;
+        for (int k = 0; k < NK; ++k) {
+            const int p = tid + k * T;
+            sites[k] = make_site(p < g.NPL ? p : 0, g.LP);
+            if (regs) {
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
                     if (p < g.NPL) st[k][c] = rng_g[base + c * gplane + p];
@@ -198,30 +331,61 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
         const float e_hi0 = cm.e_run[2 * r], e_lo0 = cm.e_run[2 * r + 1];
         const long long sweep0 = cm.clock[0];
         const int tslot = rep.ladder_start + cm.w2t[r];
-        cluster.sync();
+        cluster_arrive();
 
         float dsum = 0.0f, dcomp = 0.0f;
         int nacc = 0;
+        typename M::Prop pa[NK], pb[NK];
         for (int s = 0; s < cm.n_sweeps; ++s) {
-            colour_pass<M, NPMAX, 0>(a, ctx, cluster, cells, own, g, st, regs, base, gplane, dsum, dcomp, nacc);
-            cluster.sync();
-            colour_pass<M, NPMAX, 1>(a, ctx, cluster, cells, own, g, st, regs, base, gplane, dsum, dcomp, nacc);
-            if (M::kSplitMiddle) cluster.sync();
-            colour_pass<M, NPMAX, 2>(a, ctx, cluster, cells, own, g, st, regs, base, gplane, dsum, dcomp, nacc);
-            cluster.sync();
-            colour_pass<M, NPMAX, 3>(a, ctx, cluster, cells, own, g, st, regs, base, gplane, dsum, dcomp, nacc);
-            cluster.sync();
+            if (regs) {
+                // Invariant: this thread has arrived at the barrier that
+                // follows the previous phase and not yet waited.
+                propose_pass<M, NK, 0>(ctx, cells, own, g, sites, st, pa);
+                cluster_wait();
+                decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
+                cluster_arrive();
+                propose_pass<M, NK, 1>(ctx, cells, own, g, sites, st, pa);
+                propose_pass<M, NK, 2>(ctx, cells, own, g, sites, st, pb);
+                cluster_wait();
+                decide_pass<M, NK, 1>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
+                if (M::kSplitMiddle) {
+                    cluster_arrive();
+                    cluster_wait();
+                }
+                decide_pass<M, NK, 2>(ctx, cells, own, g, sites, pb, dsum, dcomp, nacc);
+                cluster_arrive();
+                propose_pass<M, NK, 3>(ctx, cells, own, g, sites, st, pa);
+                cluster_wait();
+                decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
+                cluster_arrive();
+            } else {
+                cluster_wait();
+                global_rng_pass<M, 0>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                cluster_arrive();
+                cluster_wait();
+                global_rng_pass<M, 1>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                if (M::kSplitMiddle) {
+                    cluster_arrive();
+                    cluster_wait();
+                }
+                global_rng_pass<M, 2>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                cluster_arrive();
+                cluster_wait();
+                global_rng_pass<M, 3>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                cluster_arrive();
+            }
 
             const int slot = sample_slot(sweep0 + s + 1, cm.first_sample_sweep, cm.sample_interval, cm.n_slots);
             if (slot >= 0 && cm.samples != nullptr) {
+                cluster_wait();
                 double v[NC];
 #pragma unroll
                 for (int q = 0; q < NC; ++q) v[q] = 0.0;
                 v[0] = M::kEnergyFromDelta ? (double)dsum + (double)dcomp : 0.0;
-                measure_colour<M, 0>(ctx, cluster, cells, own, g, v);
-                measure_colour<M, 1>(ctx, cluster, cells, own, g, v);
-                measure_colour<M, 2>(ctx, cluster, cells, own, g, v);
-                measure_colour<M, 3>(ctx, cluster, cells, own, g, v);
+                measure_colour<M, 0>(ctx, cells, own, g, v);
+                measure_colour<M, 1>(ctx, cells, own, g, v);
+                measure_colour<M, 2>(ctx, cells, own, g, v);
+                measure_colour<M, 3>(ctx, cells, own, g, v);
                 block_sum<NC>(v, scratch);
                 if (tid == 0) {
 #pragma unroll
@@ -249,17 +413,18 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
                         for (int q = 0; q < NC; ++q) out[(size_t)q * cm.n_temps_total] = tot[q];
                     }
                 }
-                cluster.sync();
+                cluster_arrive();
             }
         }
+        cluster_wait();
 
         // Window epilogue: energy and acceptance bookkeeping, write back.
         double v2[3] = {(double)dsum + (double)dcomp, (double)nacc, 0.0};
         if (M::kExactEnergy) {
-            energy_colour<M, 0>(ctx, cluster, cells, own, g, v2[2]);
-            energy_colour<M, 1>(ctx, cluster, cells, own, g, v2[2]);
-            energy_colour<M, 2>(ctx, cluster, cells, own, g, v2[2]);
-            energy_colour<M, 3>(ctx, cluster, cells, own, g, v2[2]);
+            energy_colour<M, 0>(ctx, cells, own, g, v2[2]);
+            energy_colour<M, 1>(ctx, cells, own, g, v2[2]);
+            energy_colour<M, 2>(ctx, cells, own, g, v2[2]);
+            energy_colour<M, 3>(ctx, cells, own, g, v2[2]);
         }
         block_sum<3>(v2, scratch);
         if (tid == 0) {
@@ -268,11 +433,14 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
             red[NC + 2] = v2[2];
         }
         for (int c = 0; c < 4; ++c)
-            for (int p = tid; p < g.NPL; p += T)
-                M::store(a, base + c * gplane + p, cells[c * g.NPL + p], own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
+            for (int p = tid; p < g.NPL; p += T) {
+                const Site s = make_site(p, g.LP);
+                M::store(a, base + c * gplane + p, cells[c * g.PS + s.o + s.pc],
+                         own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
+            }
         if (regs) {
 #pragma unroll
-            for (int k = 0; k < (NPMAX > 0 ? NPMAX : 1); ++k) {
+            for (int k = 0; k < NK; ++k) {
                 const int p = tid + k * T;
 #pragma unroll
                 for (int c = 0; c < 4; ++c)

@@ -12,6 +12,7 @@
 #include <stdint.h>
 
 #include "../../include/mcgb.h"
+#include "rng_convert.h"
 
 namespace mcgb {
 
@@ -53,13 +54,11 @@ __device__ __forceinline__ double xoro_uniform_f64(ulonglong2 &s)
     return (double)(xoro_next(s) >> 11) * 0x1.0p-53;
 }
 
-// float32 of the float64 uniform.  The 53-bit integer m = x >> 11 converts to
-// float32 with one round-to-nearest-even step, and the power-of-two scale is
-// exact, so RN32(m) * 2^-53 equals float32(m * 2^-53) bit for bit, without
-// a float64 operation.
+// float32 of the float64 uniform, rounded in integer arithmetic (see
+// rng_convert.h) so that no instruction issues to the float64 pipe.
 __device__ __forceinline__ float xoro_uniform_f32(ulonglong2 &s)
 {
-    return __ull2float_rn(xoro_next(s) >> 11) * 0x1.0p-53f;
+    return mcgb_unit_f32(xoro_next(s));
 }
 
 // ---------------------------------------------------------------- complex64

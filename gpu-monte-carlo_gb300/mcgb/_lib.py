@@ -47,7 +47,7 @@ SIGNATURES = {
     "mcgb_pt_exchange": [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I64, _P],
     "mcgb_pt_record_walkers": [_P, _P, _P, _I, _P],
     "mcgb_batch_channels": [_I],
-    "mcgb_batch_smem_bytes": [_I, _I64],
+    "mcgb_batch_smem_bytes": [_I, _I, _I],
     "mcgb_batch_max_clusters": [_I, _I, _I, _I64, _P],
     "mcgb_batch_window_run": [_I, _P, _P],
     "mcgb_batch_permute": [_P, _P, _I64, _P, _P, _I, _I, _I, _P],

@@ -309,8 +309,10 @@ class LadderBatch:
 
     # ------------------------------------------------------------ launch shape
     def _smem(self, C):
-        npl = max(int(L) * int(L) // (4 * C) for L in self.table_host["L"])
-        return int(_lib.load().mcgb_batch_smem_bytes(self.model_id, npl))
+        v = int(_lib.load().mcgb_batch_smem_bytes(self.model_id, int(self.max_L), int(C)))
+        if v < 0:
+            _lib.check(v, "mcgb_batch_smem_bytes")
+        return v
 
     def candidate_shapes(self):
         """(cluster_size, threads) pairs valid for every replica of the batch."""
@@ -493,6 +495,49 @@ class LadderBatch:
         _lib.call("mcgb_batch_exchange", ctypes.byref(w), ctypes.byref(self._pt()), s)
         _lib.call("mcgb_batch_clock_tick", self.clock.cptr, 0, 1, s)
         self.exchange_rounds += 1
+
+    # ------------------------------------------------------------ host I/O
+    def pinned_state_buffers(self):
+        """Pinned host byte buffers for the ladder state and RNG (engine layout)."""
+        import torch as _t
+        return {"state": _t.empty(self.state.nbytes, dtype=_t.uint8, pin_memory=True),
+                "rng": _t.empty(self.rng.nbytes, dtype=_t.uint8, pin_memory=True)}
+
+    def upload_state(self, host):
+        """Asynchronous host-to-device copy of state and RNG (engine layout) from
+        pinned buffers, then the (cos, sin) cache and exact energies."""
+        self.state.raw().copy_(host["state"], non_blocking=True)
+        self.rng.raw().copy_(host["rng"], non_blocking=True)
+        self.refresh_aux()
+        self.recompute_energy()
+
+    def download_state(self, host):
+        """Asynchronous device-to-host copy of state and RNG into pinned buffers."""
+        host["state"].copy_(self.state.raw(), non_blocking=True)
+        host["rng"].copy_(self.rng.raw(), non_blocking=True)
+
+    def checkpoint(self):
+        """Everything needed to resume the chain bit-exactly, as host arrays."""
+        names = ["state", "rng", "betas", "w2t", "t2w", "e_run", "energies", "accepted", "accepted_prev",
+                 "clock", "sigma_t", "counters"]
+        if self.aux is not None:
+            names.append("aux")
+        if self.pt:
+            names += ["pair_rng", "swap_counts", "trips"]
+        ck = {n: getattr(self, n).copy_to_host().copy() for n in names}
+        ck["sweeps"], ck["exchange_rounds"] = self.sweeps, self.exchange_rounds
+        return ck
+
+    def restore(self, ck):
+        """Resume from checkpoint(); the batch must have the same ladders."""
+        for name, value in ck.items():
+            if name in ("sweeps", "exchange_rounds"):
+                continue
+            arr = getattr(self, name)
+            if arr.nbytes != np.asarray(value).nbytes:
+                raise ValueError(f"checkpoint field {name} does not match this batch")
+            arr.copy_to_device(value)
+        self.sweeps, self.exchange_rounds = int(ck["sweeps"]), int(ck["exchange_rounds"])
 
     def refresh_aux(self):
         """Recompute the (cos, sin) cache from the state."""

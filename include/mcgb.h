@@ -209,7 +209,9 @@ typedef struct mcgb_batch_window {
     double *energies;               /* out, per replica: energy after the window */
     long long *accepted;            /* per replica: += accepted moves (He3: all sub-counters) */
     long long *counters;            /* He3 Gaussian: (3, n_replicas) attempts/accepted/nonfinite, else NULL */
-    double *samples;                /* [n_slots][channels][n_temps_total] or NULL */
+    double *samples;                /* ring of [n_slots][channels][n_temps_total] or NULL; the
+                                       sample after cumulative sweep s lands in slot
+                                       ((s - first_sample_sweep) / sample_interval) % n_slots */
     double *staging;                /* [channels][n_replicas]: when not NULL, a sample due at the
                                        window's last sweep goes here (walker order) for the exchange
                                        to scatter with the updated temperature map */
@@ -225,9 +227,9 @@ typedef struct mcgb_batch_window {
 
 /* Number of float64 sample channels a model writes per replica. */
 int mcgb_batch_channels(int model);
-/* Dynamic shared memory (bytes) a window needs for a strip of
- * max_plaquettes = max(L^2) / (4 * cluster_size). */
-int64_t mcgb_batch_smem_bytes(int model, int64_t max_plaquettes);
+/* Dynamic shared memory (bytes) a window needs when the largest lattice
+ * of the batch is max_L and clusters have cluster_size CTAs. */
+int64_t mcgb_batch_smem_bytes(int model, int max_L, int cluster_size);
 /* Largest number of co-resident clusters of `cluster_size` CTAs of `threads`
  * threads with `smem_bytes` dynamic shared memory (cudaOccupancyMaxActiveClusters). */
 int mcgb_batch_max_clusters(int model, int cluster_size, int threads, int64_t smem_bytes, int *out);
