@@ -276,6 +276,17 @@ typedef struct mcgb_batch_pt {
  * schedules them.  A staged window-end sample is then written to the slots
  * of the updated map, matching a measurement taken after the exchange. */
 int mcgb_batch_exchange(const mcgb_batch_window *w, const mcgb_batch_pt *pt, void *stream);
+/* No counterpart in the reference.  mcgb_batch_window_run then
+ * mcgb_batch_exchange in one call that allocates nothing, for callers that
+ * cannot allocate device memory (inside a CUDA-graph capture, or under a
+ * runtime that owns every device allocation).  w->staging must be NULL: the
+ * deferred-sample scratch is a fixed array in the library of 32768 doubles,
+ * so channels x n_replicas must not exceed 32768 (else MCGB_EINVAL).  All
+ * calls share that array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  The caller ticks the clock as with the two separate calls. */
+int mcgb_batch_window_exchange_noalloc(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
+                                       void *stream);
 /* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
  * a captured graph of windows and exchanges can be replayed. */
 int mcgb_batch_clock_tick(int64_t *clock, int n_sweeps, int exchanged, void *stream);
