@@ -28,6 +28,8 @@ struct IsingPolicy {
     using Cell = int8_t;
     static constexpr int kOwnFloats = 0;
     static constexpr int kChannels = 2;  // energy, magnetization
+    static constexpr int kSums = 2;
+    static constexpr int kMaxThreads = 1024;
     static constexpr bool kSplitMiddle = false;
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
@@ -115,6 +117,8 @@ struct XYPolicy {
     using Cell = float2;  // (cos theta, sin theta)
     static constexpr int kOwnFloats = 1;  // theta
     static constexpr int kChannels = 5;   // energy, mx, my, twist_cos_x, twist_sin_x
+    static constexpr int kSums = 5;
+    static constexpr int kMaxThreads = 1024;
     static constexpr bool kSplitMiddle = false;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;

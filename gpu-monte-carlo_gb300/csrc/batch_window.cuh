@@ -40,7 +40,8 @@
 //   Prop propose<c>(const Ctx&, const Cell&, const float* own, ulonglong2&)
 //   bool decide<c>(const Ctx&, Nbrs, Cell&, float* own, const Prop&, float& dE)
 //   void measure<c>(const Ctx&, Nbrs, const Cell&, const float* own, double* v)
-//   void finish_sample(const Ctx&, double* v)  (channel 0 holds the energy)
+//   void finish_sample(const Ctx&, double* v)  (turns kSums reduced sums, sum 0
+//        the energy, into the kChannels output channels, in place)
 // and two flags: kEnergyFromDelta (channel 0 = running energy + accepted
 // changes; else measure<c> accumulates it) and kExactEnergy (the epilogue
 // recomputes the energy exactly with energy_site<c>/finish_energy instead of
@@ -130,7 +131,7 @@ constexpr int kRedDoubles = 16;  // per-CTA cluster reduction slots
 template <class M>
 __host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp)
 {
-    return sizeof(double) * (kRedDoubles + 32 * (M::kChannels + 3)) +
+    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3)) +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
            (size_t)4 * npl * sizeof(float) * M::kOwnFloats;
 }
@@ -257,18 +258,21 @@ __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typena
 }
 
 // Threads per block the NPMAX variant is compiled for: NPMAX streams of four
-// colours live in registers (16 registers per plaquette).
-template <int NPMAX>
+// colours live in registers (16 registers per plaquette); policies with large
+// cells cap it with kMaxThreads.
+template <class M, int NPMAX>
 constexpr int window_max_threads()
 {
-    return NPMAX <= 1 ? 1024 : 512;
+    return (NPMAX <= 1 ? 1024 : 512) < M::kMaxThreads ? (NPMAX <= 1 ? 1024 : 512) : M::kMaxThreads;
 }
 
 template <class M, int NPMAX>
-__global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(const typename M::Args a)
+__global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kernel(const typename M::Args a)
 {
     using Cell = typename M::Cell;
-    constexpr int NC = M::kChannels;
+    constexpr int NC = M::kChannels;  // output channels
+    constexpr int NS = M::kSums;      // reduced sums (>= NC)
+    static_assert(NS + 3 <= kRedDoubles, "too many reduced sums");
     constexpr int NK = NPMAX > 0 ? NPMAX : 1;
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
@@ -278,8 +282,8 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
 
     extern __shared__ __align__(16) unsigned char smem[];
     double *red = reinterpret_cast<double *>(smem);  // kRedDoubles
-    double *scratch = red + kRedDoubles;               // 32 * (NC + 3)
-    Cell *cells = reinterpret_cast<Cell *>(scratch + 32 * (NC + 3));
+    double *scratch = red + kRedDoubles;               // 32 * (NS + 3)
+    Cell *cells = reinterpret_cast<Cell *>(scratch + 32 * (NS + 3));
 
     const WindowCommon &cm = a.c;
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
@@ -378,28 +382,28 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
             const int slot = sample_slot(sweep0 + s + 1, cm.first_sample_sweep, cm.sample_interval, cm.n_slots);
             if (slot >= 0 && cm.samples != nullptr) {
                 cluster_wait();
-                double v[NC];
+                double v[NS];
 #pragma unroll
-                for (int q = 0; q < NC; ++q) v[q] = 0.0;
+                for (int q = 0; q < NS; ++q) v[q] = 0.0;
                 v[0] = M::kEnergyFromDelta ? (double)dsum + (double)dcomp : 0.0;
                 measure_colour<M, 0>(ctx, cells, own, g, v);
                 measure_colour<M, 1>(ctx, cells, own, g, v);
                 measure_colour<M, 2>(ctx, cells, own, g, v);
                 measure_colour<M, 3>(ctx, cells, own, g, v);
-                block_sum<NC>(v, scratch);
+                block_sum<NS>(v, scratch);
                 if (tid == 0) {
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) red[q] = v[q];
+                    for (int q = 0; q < NS; ++q) red[q] = v[q];
                 }
                 cluster.sync();
                 if (rank == 0 && tid == 0) {
-                    double tot[NC];
+                    double tot[NS];
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) tot[q] = 0.0;
+                    for (int q = 0; q < NS; ++q) tot[q] = 0.0;
                     for (int k = 0; k < C; ++k) {
                         const double *rr = cluster.map_shared_rank(red, k);
 #pragma unroll
-                        for (int q = 0; q < NC; ++q) tot[q] += rr[q];
+                        for (int q = 0; q < NS; ++q) tot[q] += rr[q];
                     }
                     if (M::kEnergyFromDelta) tot[0] += (double)e_hi0 + (double)e_lo0;
                     M::finish_sample(ctx, tot);
@@ -428,9 +432,9 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
         }
         block_sum<3>(v2, scratch);
         if (tid == 0) {
-            red[NC] = v2[0];
-            red[NC + 1] = v2[1];
-            red[NC + 2] = v2[2];
+            red[NS] = v2[0];
+            red[NS + 1] = v2[1];
+            red[NS + 2] = v2[2];
         }
         for (int c = 0; c < 4; ++c)
             for (int p = tid; p < g.NPL; p += T) {
@@ -452,9 +456,9 @@ __global__ void __launch_bounds__(window_max_threads<NPMAX>(), 1) window_kernel(
             double de = 0.0, na = 0.0, ex = 0.0;
             for (int k = 0; k < C; ++k) {
                 const double *rr = cluster.map_shared_rank(red, k);
-                de += rr[NC];
-                na += rr[NC + 1];
-                ex += rr[NC + 2];
+                de += rr[NS];
+                na += rr[NS + 1];
+                ex += rr[NS + 2];
             }
             float hi, lo2;
             if (M::kExactEnergy) {

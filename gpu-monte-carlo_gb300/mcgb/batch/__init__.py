@@ -325,8 +325,9 @@ class LadderBatch:
             if smem > 232448:
                 continue
             npl_max = int(self.max_L) ** 2 // (4 * C)
+            t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512}.get(self.model_id, 1024)
             for T in (128, 256, 512, 1024):
-                if T > 32 * ((npl_max + 31) // 32) and T > 128:
+                if T > t_max or (T > 32 * ((npl_max + 31) // 32) and T > 128):
                     continue
                 out.append((C, T))
         return out
@@ -630,6 +631,23 @@ class LadderBatch:
     def acceptance(self):
         """Accepted moves per replica so far (device counters)."""
         return self.accepted.copy_to_host()
+
+    def sampling_diagnostics(self):
+        """He3 Gaussian sampler counters per replica (walker order), in the
+        keys of models/he3/gaussian_fast.py:147-156."""
+        L2 = self.table_host["L"].astype(np.int64) ** 2
+        attempts = L2 * self.sweeps
+        accepted = self.accepted.copy_to_host()
+        nonfinite = self.counters.copy_to_host()[2]
+        return {
+            "algorithm": "float32_conditional_gaussian_full_hamiltonian_mh",
+            "sweeps_including_compilation": self.sweeps,
+            "rho": self.rho, "proposal_mass": self.mass,
+            "attempts": attempts.tolist(), "accepted": accepted.tolist(),
+            "nonfinite_rejections": nonfinite.tolist(),
+            "acceptance_rates": np.divide(accepted, attempts, out=np.zeros(self.R),
+                                          where=attempts > 0).tolist(),
+        }
 
     # ------------------------------------------------------------ autotuning
     def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False):

@@ -176,3 +176,113 @@ def test_invalid_batches_raise():
         LadderBatch(IsingModel(), [(16, [2.0])], exchange_interval=10)
     with pytest.raises(ValueError):
         LadderBatch(IsingModel(), [(16, [2.0, 3.0])], cluster_size=16, threads=128)
+
+
+# ------------------------------------------------------------ Kawamura and He3
+
+def assert_close_sites(got, ref, axes, tol=1e-4, max_frac=2e-3):
+    d = np.abs(got.astype(np.complex128) - ref.astype(np.complex128))
+    if axes:
+        d = d.max(axis=axes)
+    assert np.mean(d > tol) <= max_frac, f"{int(np.sum(d > tol))} of {d.size} sites differ"
+
+
+def test_kawamura_batch_sweep_matches_oracle_and_tracks_energy():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.kawamura.model import KawamuraModel
+    L, temps = 32, np.linspace(0.65, 0.8, 4)
+    init = npref.random_kawamura(np.random.default_rng(9), 4, L)
+    b = LadderBatch(KawamuraModel(), [(L, temps)], seeds=[8], exchange_interval=None, cluster_size=2,
+                    threads=256, initial_states=[init])
+    e0 = b.energies.copy_to_host()
+    np.testing.assert_allclose(e0, npref.kawamura(init, 1.0)["energy"], rtol=1e-10, atol=1e-9)
+    b.run(1)
+    ref, rr = init.copy(), oracle.rng_states(4 * L * L, 8)
+    betas = (1 / temps).astype(np.float32)
+    for c in range(4):
+        oracle.kawamura_update_color(ref, rr, betas, c, np.float32(1), np.float32(1.5))
+    np.testing.assert_array_equal(b.ladder_rng(0), rr)
+    got = b.ladder_state(0)
+    assert_close_sites(got, ref, -1)
+    d_run = b.energies.copy_to_host() - e0
+    d_exact = npref.kawamura(got, 1.0)["energy"] - e0
+    assert np.all(np.abs(d_run - d_exact) <= 1e-5 * np.abs(d_exact))
+    b.run(40)
+    drift = b.recompute_energy().copy_to_host()
+    assert np.all(np.abs(drift) <= 1e-5 * np.abs(b.energies.copy_to_host()))
+    st = b.ladder_state(0)
+    np.testing.assert_allclose(np.linalg.norm(st[..., 2:], axis=-1), 1, atol=3e-6)
+    assert set(np.unique(st[..., 1])) <= {-1.0, 1.0}
+
+
+def test_kawamura_batch_pt_samples_match_numpy():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.kawamura.model import KawamuraModel
+    L, temps = 16, np.linspace(0.65, 0.8, 5)
+    b = LadderBatch(KawamuraModel(J=1.1), [(L, temps), (32, temps[:3])], exchange_interval=3, cluster_size=2,
+                    threads=128)
+    runs = b.simulate(thermalization_sweeps=5, measurement_sweeps=12, sample_interval=6)
+    for k, (Lk, Tk) in enumerate(b.ladders):
+        last = {name: v[-1] for name, v in runs[k]["samples"].items()}
+        st = b.ladder_state(k)
+        ref = npref.kawamura(st, 1.1)
+        order = b.w2t.copy_to_host()[b.ladder_starts_host[k]:b.ladder_starts_host[k] + len(Tk)]
+        for name in ref:
+            want = np.empty(len(Tk))
+            want[order] = ref[name]
+            np.testing.assert_allclose(last[name], want, rtol=1e-5, atol=2e-3 * Lk * Lk ** 0.5, err_msg=name)
+        assert sum(runs[k]["metadata"]["parallel_tempering"]["attempts"]) > 0
+
+
+@pytest.mark.parametrize("gaussian", [False, True])
+def test_he3_batch_sweep_matches_oracle_and_tracks_energy(gaussian):
+    from mcgb.batch import LadderBatch
+    from mcgb.models.he3.model import He3Model
+    L, temps = 16, np.array([0.3, 0.4, 0.6])
+    model = He3Model(pressure=20, g_d=0.001)
+    init = npref.random_he3(np.random.default_rng(4), (3, L, L, 3, 2))
+    b = LadderBatch(model, [(L, temps)], seeds=[227], exchange_interval=None, gaussian=gaussian,
+                    cluster_size=2, threads=128, initial_states=[init])
+    e0 = b.energies.copy_to_host()
+    np.testing.assert_allclose(e0, npref.he3_energy(init, float(model.K), model.betas, g_d=float(model.g_d)),
+                               rtol=1e-9, atol=1e-9)
+    b.run(1)
+    ref, rr = init.copy(), oracle.rng_states(3 * L * L, 227)
+    betas = (1 / temps).astype(np.float32)
+    counts = np.zeros((3, 3, L, L), np.int64)
+    for c in range(4):
+        if gaussian:
+            oracle.he3_gaussian_update_color(ref, rr, betas, c, model.betas, model.K, np.float32(-0.9),
+                                             np.float32(0), model.g_d, counts)
+        else:
+            oracle.he3_update_color(ref, rr, betas, c, model.betas, model.K, model.delta, model.g_d)
+    np.testing.assert_array_equal(b.ladder_rng(0), rr)
+    got = b.ladder_state(0)
+    assert_close_sites(got, ref, (-2, -1))
+    d_run = b.energies.copy_to_host() - e0
+    d_exact = npref.he3_energy(got, float(model.K), model.betas, g_d=float(model.g_d)) - e0
+    assert np.all(np.abs(d_run - d_exact) <= 1e-5 * np.abs(d_exact) + 1e-4)
+    b.run(20)
+    drift = b.recompute_energy().copy_to_host()
+    assert np.all(np.abs(drift) <= 1e-5 * np.maximum(np.abs(b.energies.copy_to_host()), L * L))
+    if gaussian:
+        d = b.sampling_diagnostics()
+        assert sum(d["nonfinite_rejections"]) == 0 and 0 < sum(d["accepted"]) < sum(d["attempts"])
+
+
+def test_he3_ragged_batch_samples_match_numpy():
+    from mcgb.batch import LadderBatch
+    from mcgb.models.he3.model import He3Model
+    model = He3Model(pressure=20)
+    ladders = [(16, [0.33, 0.4, 0.47]), (32, [0.33, 0.4, 0.47])]
+    b = LadderBatch(model, ladders, exchange_interval=2, gaussian=True)
+    runs = b.simulate(thermalization_sweeps=4, measurement_sweeps=6, sample_interval=6)
+    for k, (Lk, Tk) in enumerate(b.ladders):
+        last = {name: v[-1] for name, v in runs[k]["samples"].items()}
+        st = b.ladder_state(k)
+        ref = npref.he3(st, float(model.K), model.betas)
+        order = b.w2t.copy_to_host()[b.ladder_starts_host[k]:b.ladder_starts_host[k] + len(Tk)]
+        for name in ref:
+            want = np.empty(len(Tk))
+            want[order] = ref[name]
+            np.testing.assert_allclose(last[name], want, rtol=2e-5, atol=1e-3 * Lk, err_msg=name)
