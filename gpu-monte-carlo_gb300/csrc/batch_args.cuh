@@ -54,8 +54,8 @@ inline BatchArgs make_args(const mcgb_batch_window &w)
     return a;
 }
 
-// Largest L of the batch, after validating the table against the cluster
-// shape.  Returns a negative status on error.
+// Validate the table against the cluster shape.  Returns a negative status
+// on error, else 0; strips are sized per replica by effective_cluster.
 inline int validate_window(const mcgb_batch_window &w)
 {
     MCGB_REQUIRE(w.table && w.host_table && w.work_ptr && w.work_idx, "batch window: null table/work list");
@@ -68,30 +68,45 @@ inline int validate_window(const mcgb_batch_window &w)
     MCGB_REQUIRE(w.n_sweeps >= 0, "batch window: n_sweeps must be >= 0");
     MCGB_REQUIRE(w.samples == nullptr || (w.n_slots >= 1 && w.n_temps_total >= 1 && w.sample_interval >= 1),
                  "batch window: bad sample buffer");
-    int max_L = 0;
     for (int r = 0; r < w.n_replicas; ++r) {
         const mcgb_replica &rep = w.host_table[r];
-        MCGB_REQUIRE(rep.L >= 4 && rep.L % (2 * w.cluster_size) == 0,
-                     "batch window: replica %d has L=%d, not a multiple of 2*cluster_size=%d", r, rep.L,
-                     2 * w.cluster_size);
+        MCGB_REQUIRE(rep.L >= 4 && rep.L % 2 == 0 && rep.L <= 32768, "batch window: replica %d has bad L=%d", r,
+                     rep.L);
         MCGB_REQUIRE(rep.ladder_start >= 0 && rep.ladder_start + rep.n_temps <= w.n_replicas &&
                          rep.ladder_start <= r && r < rep.ladder_start + rep.n_temps,
                      "batch window: replica %d has an inconsistent ladder range", r);
         MCGB_REQUIRE(rep.state_offset >= 0, "batch window: negative state offset");
-        if (rep.L > max_L) max_L = rep.L;
     }
     MCGB_REQUIRE(w.samples == nullptr || w.n_temps_total >= w.n_replicas,
                  "batch window: n_temps_total must cover every replica");
-    return max_L;
+    return MCGB_OK;
+}
+
+// Shared memory for the largest strip of the batch.
+template <class M>
+inline size_t batch_smem(const mcgb_replica *table, int n, int C)
+{
+    size_t best = 0;
+    for (int r = 0; r < n; ++r) {
+        const int L = table[r].L, Ce = effective_cluster(L, C);
+        const size_t b = window_smem_bytes<M>((long long)L * L / (4 * Ce), (long long)L / 2);
+        if (b > best) best = b;
+    }
+    return best;
+}
+
+template <class M>
+inline size_t single_smem(int L, int C)
+{
+    const int Ce = effective_cluster(L, C);
+    return window_smem_bytes<M>((long long)L * L / (4 * Ce), (long long)L / 2);
 }
 
 template <class M, int NPMAX>
-int launch_window(const BatchArgs &a, const mcgb_batch_window &w, int max_L, cudaStream_t stream,
-                  const char *name)
+int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t stream, const char *name)
 {
     auto kern = window_kernel<M, NPMAX>;
-    const size_t smem =
-        window_smem_bytes<M>((long long)max_L * max_L / (4 * w.cluster_size), (long long)max_L / 2);
+    const size_t smem = batch_smem<M>(w.host_table, w.n_replicas, w.cluster_size);
     MCGB_REQUIRE(smem <= 232448, "%s: a strip needs %zu bytes of shared memory (> 227 KB); use a larger "
                                  "cluster_size", name, smem);
     int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),

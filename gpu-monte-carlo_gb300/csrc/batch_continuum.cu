@@ -559,32 +559,35 @@ __global__ void batch_energy64_continuum(int model, const void *state, const mcg
 // Both register variants are compiled for kMaxThreads threads per CTA; the
 // two-plaquette variant serves strips of up to 2 * threads plaquettes.
 template <class M>
-int continuum_launch(const BatchArgs &a, const mcgb_batch_window &w, int max_L, cudaStream_t s, const char *name)
+int continuum_launch(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s, const char *name)
 {
     MCGB_REQUIRE(w.threads <= M::kMaxThreads, "%s: at most %d threads per CTA", name, M::kMaxThreads);
-    const long long npl = (long long)max_L * max_L / (4 * w.cluster_size);
-    if (npl <= w.threads) return launch_window<M, 1>(a, w, max_L, s, name);
-    return launch_window<M, 2>(a, w, max_L, s, name);
+    long long npl = 0;
+    for (int r = 0; r < w.n_replicas; ++r) {
+        const int L = w.host_table[r].L;
+        const long long n = (long long)L * L / (4 * effective_cluster(L, w.cluster_size));
+        if (n > npl) npl = n;
+    }
+    if (npl <= w.threads) return launch_window<M, 1>(a, w, s, name);
+    return launch_window<M, 2>(a, w, s, name);
 }
 
 int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s)
 {
-    const int max_L = validate_window(w);
-    if (max_L < 0) return max_L;
+    if (int st = validate_window(w)) return st;
     MCGB_REQUIRE(model != MCGB_MODEL_KAWAMURA || w.aux != nullptr, "Kawamura window: null (cos, sin) cache");
     const BatchArgs a = make_args(w);
     switch (model) {
-    case MCGB_MODEL_KAWAMURA: return continuum_launch<KawamuraPolicy>(a, w, max_L, s, "kawamura window");
-    case MCGB_MODEL_HE3: return continuum_launch<He3Policy<false>>(a, w, max_L, s, "he3 window");
-    default: return continuum_launch<He3Policy<true>>(a, w, max_L, s, "he3 gaussian window");
+    case MCGB_MODEL_KAWAMURA: return continuum_launch<KawamuraPolicy>(a, w, s, "kawamura window");
+    case MCGB_MODEL_HE3: return continuum_launch<He3Policy<false>>(a, w, s, "he3 window");
+    default: return continuum_launch<He3Policy<true>>(a, w, s, "he3 gaussian window");
     }
 }
 
-int64_t continuum_smem(int model, int max_L, int C)
+int64_t continuum_smem(int model, int L, int C)
 {
-    const long long npl = (long long)max_L * max_L / (4 * C), lp = max_L / 2;
-    if (model == MCGB_MODEL_KAWAMURA) return (int64_t)window_smem_bytes<KawamuraPolicy>(npl, lp);
-    return (int64_t)window_smem_bytes<He3Policy<false>>(npl, lp);
+    if (model == MCGB_MODEL_KAWAMURA) return (int64_t)single_smem<KawamuraPolicy>(L, C);
+    return (int64_t)single_smem<He3Policy<false>>(L, C);
 }
 
 template <class M>

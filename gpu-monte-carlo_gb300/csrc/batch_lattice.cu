@@ -284,21 +284,18 @@ int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s)
 int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s)
 {
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w.aux != nullptr, "XY window: null (cos, sin) cache");
-    const int max_L = validate_window(w);
-    if (max_L < 0) return max_L;
+    if (int st = validate_window(w)) return st;
     const BatchArgs a = make_args(w);
     if (model == MCGB_MODEL_ISING)
-        return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, max_L, s, "ising window")
-                               : launch_window<IsingPolicy, 2>(a, w, max_L, s, "ising window");
-    return w.threads > 512 ? launch_window<XYPolicy, 1>(a, w, max_L, s, "xy window")
-                           : launch_window<XYPolicy, 2>(a, w, max_L, s, "xy window");
+        return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, s, "ising window")
+                               : launch_window<IsingPolicy, 2>(a, w, s, "ising window");
+    return w.threads > 512 ? launch_window<XYPolicy, 1>(a, w, s, "xy window")
+                           : launch_window<XYPolicy, 2>(a, w, s, "xy window");
 }
 
-int64_t lattice_smem(int model, int max_L, int C)
+int64_t lattice_smem(int model, int L, int C)
 {
-    const long long npl = (long long)max_L * max_L / (4 * C), lp = max_L / 2;
-    return (int64_t)(model == MCGB_MODEL_ISING ? window_smem_bytes<IsingPolicy>(npl, lp)
-                                               : window_smem_bytes<XYPolicy>(npl, lp));
+    return (int64_t)(model == MCGB_MODEL_ISING ? single_smem<IsingPolicy>(L, C) : single_smem<XYPolicy>(L, C));
 }
 
 int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out)

@@ -162,12 +162,12 @@ extern "C" int mcgb_batch_channels(int model)
     }
 }
 
-extern "C" int64_t mcgb_batch_smem_bytes(int model, int max_L, int cluster_size)
+extern "C" int64_t mcgb_batch_smem_bytes(int model, int L, int cluster_size)
 {
     MCGB_REQUIRE(known_model(model), "unknown model %d", model);
     MCGB_REQUIRE(cluster_size >= 1 && cluster_size <= 16, "cluster_size must be 1..16");
-    MCGB_REQUIRE(max_L >= 4 && max_L % (2 * cluster_size) == 0, "max_L must be a multiple of 2 * cluster_size");
-    return is_lattice(model) ? lattice_smem(model, max_L, cluster_size) : continuum_smem(model, max_L, cluster_size);
+    MCGB_REQUIRE(L >= 4 && L % 2 == 0, "L must be even and >= 4");
+    return is_lattice(model) ? lattice_smem(model, L, cluster_size) : continuum_smem(model, L, cluster_size);
 }
 
 extern "C" int mcgb_batch_max_clusters(int model, int cluster_size, int threads, int64_t smem_bytes, int *out)

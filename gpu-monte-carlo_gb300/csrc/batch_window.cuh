@@ -140,6 +140,18 @@ struct StripCtx {
     int LP, HP, NPL, PS, up, dn;
 };
 
+// CTAs of a C-CTA cluster that hold a replica of size L: the largest divisor
+// of L/2 (the plaquette rows) that does not exceed C.  The other CTAs of the
+// cluster hold no rows of that replica and only take part in the barriers,
+// so one cluster shape serves every L of a ragged batch.
+__host__ __device__ __forceinline__ int effective_cluster(int L, int C)
+{
+    const int rows = L >> 1;
+    for (int c = C; c > 1; --c)
+        if (rows % c == 0) return c;
+    return 1;
+}
+
 // After an accepted move on a boundary plaquette, copy the new cell into the
 // halo of the neighbouring CTA that reads it.
 template <int C_, typename Cell>
@@ -293,13 +305,14 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     for (int w = cm.work_ptr[cid]; w < cm.work_ptr[cid + 1]; ++w) {
         const int r = cm.work_idx[w];
         const mcgb_replica rep = cm.table[r];
+        const int Ce = effective_cluster(rep.L, C);
         StripCtx g;
         g.LP = rep.L >> 1;
-        g.HP = rep.L / (2 * C);
+        g.HP = rank < Ce ? rep.L / (2 * Ce) : 0;
         g.NPL = g.HP * g.LP;
         g.PS = (g.HP + 2) * g.LP;
-        g.up = rank == 0 ? C - 1 : rank - 1;
-        g.dn = rank + 1 == C ? 0 : rank + 1;
+        g.up = rank == 0 ? Ce - 1 : rank - 1;
+        g.dn = rank + 1 >= Ce ? 0 : rank + 1;
         float *own = reinterpret_cast<float *>(
             (reinterpret_cast<uintptr_t>(cells + 4 * g.PS) + 15) & ~static_cast<uintptr_t>(15));
         const int64_t gplane = (int64_t)g.LP * g.LP;

@@ -309,28 +309,43 @@ class LadderBatch:
 
     # ------------------------------------------------------------ launch shape
     def _smem(self, C):
-        v = int(_lib.load().mcgb_batch_smem_bytes(self.model_id, int(self.max_L), int(C)))
-        if v < 0:
-            _lib.check(v, "mcgb_batch_smem_bytes")
-        return v
+        best = 0
+        for L in np.unique(self.table_host["L"]):
+            v = int(_lib.load().mcgb_batch_smem_bytes(self.model_id, int(L), int(C)))
+            if v < 0:
+                _lib.check(v, "mcgb_batch_smem_bytes")
+            best = max(best, v)
+        return best
+
+    @staticmethod
+    def effective_cluster(L, C):
+        """CTAs of a C-CTA cluster that hold a replica of size L."""
+        rows = int(L) // 2
+        for c in range(int(C), 1, -1):
+            if rows % c == 0:
+                return c
+        return 1
 
     def candidate_shapes(self):
         """(cluster_size, threads) pairs valid for every replica of the batch."""
         out = []
         Ls = self.table_host["L"]
         for C in (1, 2, 4, 8, 16):
-            if np.any(Ls % (2 * C)):
-                continue
             smem = self._smem(C)
             if smem > 232448:
                 continue
-            npl_max = int(self.max_L) ** 2 // (4 * C)
+            npl_max = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in np.unique(Ls))
             t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512}.get(self.model_id, 1024)
             for T in (128, 256, 512, 1024):
                 if T > t_max or (T > 32 * ((npl_max + 31) // 32) and T > 128):
                     continue
                 out.append((C, T))
         return out
+
+    def _costs(self, C):
+        """Relative time a cluster spends on each replica (sites per active CTA)."""
+        Ls = self.table_host["L"].astype(np.int64)
+        return np.array([L * L / self.effective_cluster(L, C) for L in Ls], dtype=np.float64)
 
     def max_clusters(self, C, T):
         n = ctypes.c_int(0)
@@ -351,9 +366,9 @@ class LadderBatch:
                     continue
                 ncl = min(m, self.R)
                 # Estimated window time ~ (largest cluster load) / threads.
-                costs = self.table_host["L"].astype(np.float64) ** 2 / C
+                costs = self._costs(C)
                 _, _, loads = lpt_work_lists(costs, ncl)
-                npl = int(self.max_L) ** 2 // (4 * C)
+                npl = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in np.unique(self.table_host["L"]))
                 occupancy = min(1.0, npl / T)
                 score = loads.max() / (T * occupancy) + 0.02 * C
                 if best is None or score < best[0]:
@@ -361,8 +376,8 @@ class LadderBatch:
             if best is None:
                 raise ValueError("no cluster shape fits this batch")
             _, cluster_size, threads = best
-        if np.any(self.table_host["L"] % (2 * int(cluster_size))):
-            raise ValueError(f"every L must be a multiple of 2 * cluster_size = {2 * int(cluster_size)}")
+        if int(cluster_size) not in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16):
+            raise ValueError("cluster_size must be 1..16")
         if self._smem(int(cluster_size)) > 232448:
             raise ValueError("a strip does not fit in shared memory; use a larger cluster_size")
         self.cluster_size, self.threads = int(cluster_size), int(threads)
@@ -370,8 +385,7 @@ class LadderBatch:
         if m < 1:
             raise ValueError(f"cluster shape ({cluster_size}, {threads}) cannot be resident")
         self.n_clusters = min(m, self.R)
-        costs = self.table_host["L"].astype(np.float64) ** 2
-        wp, wi, _ = lpt_work_lists(costs, self.n_clusters)
+        wp, wi, _ = lpt_work_lists(self._costs(self.cluster_size), self.n_clusters)
         self.work_ptr, self.work_idx = to_device(wp), to_device(wi)
         self._graphs.clear()
 

@@ -184,7 +184,8 @@ enum {
 };
 
 typedef struct mcgb_replica {
-    int32_t L;             /* even; divisible by 2 * cluster_size */
+    int32_t L;             /* even, >= 4; held by the largest divisor of L/2 not above
+                              cluster_size CTAs of a cluster (the others idle for it) */
     int32_t ladder;        /* ladder index */
     int32_t ladder_start;  /* first replica index (= temperature slot 0) of the ladder */
     int32_t n_temps;       /* replicas in the ladder */
@@ -227,9 +228,9 @@ typedef struct mcgb_batch_window {
 
 /* Number of float64 sample channels a model writes per replica. */
 int mcgb_batch_channels(int model);
-/* Dynamic shared memory (bytes) a window needs when the largest lattice
- * of the batch is max_L and clusters have cluster_size CTAs. */
-int64_t mcgb_batch_smem_bytes(int model, int max_L, int cluster_size);
+/* Dynamic shared memory (bytes) a window needs for a replica of size L in
+ * clusters of cluster_size CTAs (a batch needs the maximum over its L). */
+int64_t mcgb_batch_smem_bytes(int model, int L, int cluster_size);
 /* Largest number of co-resident clusters of `cluster_size` CTAs of `threads`
  * threads with `smem_bytes` dynamic shared memory (cudaOccupancyMaxActiveClusters). */
 int mcgb_batch_max_clusters(int model, int cluster_size, int threads, int64_t smem_bytes, int *out);

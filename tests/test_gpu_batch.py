@@ -175,7 +175,25 @@ def test_invalid_batches_raise():
     with pytest.raises(ValueError):
         LadderBatch(IsingModel(), [(16, [2.0])], exchange_interval=10)
     with pytest.raises(ValueError):
-        LadderBatch(IsingModel(), [(16, [2.0, 3.0])], cluster_size=16, threads=128)
+        LadderBatch(IsingModel(), [(16, [2.0, 3.0])], cluster_size=17, threads=128)
+
+
+def test_effective_cluster_serves_lattices_smaller_than_the_cluster():
+    """L=12 in clusters of 16 CTAs: 6 plaquette rows -> 6 CTAs hold it, 10 idle."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    ladders = [(12, [2.0, 2.5]), (64, [2.0, 2.5]), (10, [2.2, 2.3])]
+    rng = np.random.default_rng(12)
+    inits = [seeded_spins(rng, 2, L) for L, _ in ladders]
+    b = LadderBatch(IsingModel(), ladders, seeds=[1, 2, 3], exchange_interval=None, cluster_size=16,
+                    threads=128, initial_states=inits)
+    assert [b.effective_cluster(L, 16) for L, _ in ladders] == [6, 16, 5]
+    b.run(9)
+    for k, (L, T) in enumerate(ladders):
+        rt = dropin_ising(L, T, [1, 2, 3][k], inits[k])
+        for _ in range(9):
+            rt.sweep()
+        np.testing.assert_array_equal(b.ladder_state(k), rt.snapshot())
 
 
 # ------------------------------------------------------------ Kawamura and He3
@@ -286,3 +304,19 @@ def test_he3_ragged_batch_samples_match_numpy():
             want = np.empty(len(Tk))
             want[order] = ref[name]
             np.testing.assert_allclose(last[name], want, rtol=2e-5, atol=1e-3 * Lk, err_msg=name)
+
+
+def test_streams_in_global_memory_path_is_bit_exact():
+    """Strips with more plaquettes than two per thread keep the RNG streams in
+    global memory (the large-L path); Ising stays bit-identical."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    L, temps = 64, [2.0, 2.4]
+    init = seeded_spins(np.random.default_rng(3), 2, L)
+    b = LadderBatch(IsingModel(), [(L, temps)], seeds=[99], exchange_interval=None, cluster_size=1,
+                    threads=128, initial_states=[init])
+    b.run(12)
+    rt = dropin_ising(L, temps, 99, init)
+    for _ in range(12):
+        rt.sweep()
+    np.testing.assert_array_equal(b.ladder_state(0), rt.snapshot())
