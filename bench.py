@@ -60,6 +60,24 @@ def initial_angles(seed):
     return np.clip(theta, np.float32(-np.pi), np.nextafter(np.float32(np.pi), np.float32(0)))
 
 
+def profiled_traffic():
+    """DRAM bytes per window launch from the committed ncu summary of the
+    window kernel on this workload (dram__bytes_read.sum + write.sum), or None."""
+    path = ROOT / "profiles" / "window_kernel_xy_L128x32.md"
+    if not path.exists():
+        return None
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    total = 0.0
+    found = 0
+    for line in path.read_text().splitlines():
+        for key in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            if f"(`{key}`)" in line:
+                fields = line.split("|")[2].split()
+                total += float(fields[0]) * scale.get(fields[1] if len(fields) > 1 else "byte", 1)
+                found += 1
+    return total if found == 2 else None
+
+
 def load_peaks():
     path = ROOT / "MEASURED_PEAKS.json"
     if path.exists():
@@ -320,7 +338,8 @@ def run_mcgb(args, rank, world):
             "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": profiled_traffic(),
+                         "traffic_source": "profiles/window_kernel_xy_L128x32.md (one ncu capture)",
                          "kernel": "window_kernel<XYPolicy>", "kernel_ms": window_ms,
                          "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind},
             "clocks": clk,
@@ -404,7 +423,7 @@ def profile_windows(cluster_size=4, threads=1024):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["mcgb", "reference"], default="mcgb")
     ap.add_argument("--skip-plain", action="store_true", help="do not time the plain FP64 form")
