@@ -15,6 +15,9 @@ Arms:
                     restatement of its kernels (the reference has no CPU sweep
                     of its own), OpenMP over replicas, a bounded sample.
 
+`value` is the production mode (updates + exchange + sampling); `modes` adds
+the same ladder with updates only and with updates + exchange.
+
 Under torchrun each rank runs its own independent ladder (seeded by rank):
 ladders share nothing, so the work shards with no data-path collective
 (weak scaling); the timing takes the max over ranks.
@@ -173,6 +176,27 @@ def cpu_sample(n_threads, sweeps, seed=7):
     return R * L * L * sweeps / (dt * 1e9), dt
 
 
+def ladder_seed(rank):
+    """Seed of rank `rank`'s ladder: the 42 + L convention, offset per rank so
+    that every rank samples an independent chain."""
+    return 42 + L + 1000 * rank
+
+
+def max_over_ranks(x, dist, device):
+    """The job's time is the slowest rank's: all-reduce MAX (identity on one rank)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world, updates_per_step, steps, total_ms):
+    """Whole-job updates/ns: every rank did `steps` steps within `total_ms`."""
+    return world * updates_per_step * steps / (total_ms * 1e6)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -228,7 +252,7 @@ def run_mcgb(args, rank, world):
             dist.barrier()
 
     temps = temperatures()
-    seed = 42 + L + 1000 * rank
+    seed = ladder_seed(rank)
     batch = LadderBatch(XYModel(J=1.0), [(L, temps)], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
                         proposal="gaussian", sigma0=1.0, initial_states=[initial_angles(seed)])
     batch.autotune()
@@ -261,12 +285,36 @@ def run_mcgb(args, rank, world):
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    total_ms = float(np.sum(step_ms))
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * updates_per_step * args.steps / (total_ms * 1e6)
+    total_ms = max_over_ranks(np.sum(step_ms), dist, "cuda")
+    value = aggregate_rate(world, updates_per_step, args.steps, total_ms)
+
+    # The same ladder in the profiler's three modes (profiling/profile_he3.py):
+    # updates only (no exchange, no samples), + replica exchange, + sampling
+    # (the timed steps above).  Bounded to 50 steps each.
+    def mode_rate(b):
+        n = min(args.steps, 50)
+        b.run(SWEEPS_PER_STEP)
+        ms = []
+        for _ in range(n):
+            flush.fill_(1)
+            m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            m0.record(stream)
+            b.run(SWEEPS_PER_STEP)
+            m1.record(stream)
+            m1.synchronize()
+            ms.append(m0.elapsed_time(m1))
+        return aggregate_rate(world, updates_per_step, n, max_over_ranks(np.sum(ms), dist, "cuda"))
+
+    saved_samples = batch.samples
+    batch.samples = None
+    pt_rate = mode_rate(batch)
+    batch.samples = saved_samples
+    plain_ladder = LadderBatch(XYModel(J=1.0), [(L, temps)], seeds=[seed], exchange_interval=None,
+                               proposal="gaussian", cluster_size=batch.cluster_size, threads=batch.threads,
+                               initial_states=[batch.ladder_state(0)])
+    plain_ladder.sigma_t.copy_to_device(sigma)
+    updates_rate = mode_rate(plain_ladder)
+    del plain_ladder
 
     # Dominant kernel: the window kernel, timed alone on the same stream.
     from mcgb import _lib
@@ -312,12 +360,8 @@ def run_mcgb(args, rank, world):
             e2e_ms.append(e0.elapsed_time(e1))
     h2d = sum(t.numel() for t in host.values())
     d2h = sum(t.numel() for t in out.values()) + out_samples.numel()
-    e2e_total = float(np.sum(e2e_ms))
-    if dist is not None:
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * updates_per_step * args.steps / (e2e_total * 1e6)
+    e2e_total = max_over_ranks(np.sum(e2e_ms), dist, "cuda")
+    e2e_value = aggregate_rate(world, updates_per_step, args.steps, e2e_total)
 
     # Plain FP64 form on the same ladder (one lattice per launch), bounded.
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
@@ -337,6 +381,8 @@ def run_mcgb(args, rank, world):
                        "parallelism": f"independent ladders x{world}"},
             "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
+            "modes": {"updates": updates_rate, "pt": pt_rate, "production": value,
+                      "unit": "updates/ns", "note": "updates only / + exchange every 10 / + sample every 10"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(),
                          "traffic_source": "profiles/window_kernel_xy_L128x32.md (one ncu capture)",
@@ -354,49 +400,25 @@ def run_mcgb(args, rank, world):
 
 
 def plain_fp64_rate(batch, sigma, seed):
-    """The plain form: every replica in its own launches (4 colours), float64
-    angles, float64 Gaussian proposals and exponentials; the exchange energies
-    from a float64 reduction per lattice.  Times 20 sweeps with 2 exchanges."""
+    """The plain form (mcgb.plain64.PlainXYLadder): every replica in its own
+    launches (4 colours), float64 angles, float64 Gaussian proposals and
+    exponentials, the exchange energies from a float64 reduction per lattice.
+    Times 20 sweeps with 2 exchanges."""
     import torch
 
-    from mcgb import _lib, device
-    from mcgb.rng import create_xoroshiro128p_states
+    from mcgb.plain64 import PlainXYLadder
 
-    R = N_TEMPS
-    theta = device.to_device(initial_angles(seed).astype(np.float64))
-    rng = create_xoroshiro128p_states(R * L * L, seed)
-    betas64 = device.to_device(1.0 / temperatures())
-    betas32 = device.to_device((1.0 / temperatures()).astype(np.float32))
-    sig = device.to_device(sigma.astype(np.float64))
-    energies = device.device_zeros(R, np.float64)
-    w2t = device.to_device(np.arange(R, dtype=np.int32))
-    t2w = device.to_device(np.arange(R, dtype=np.int32))
-    prng = create_xoroshiro128p_states(R - 1, seed + 1)
-    counts = device.device_zeros((3, R - 1), np.int64)
-    trips = device.to_device(np.zeros((5, R), np.int64))
-    s = _lib.stream_handle()
-
-    def sweeps(n, start):
-        for k in range(n):
-            for r in range(R):
-                for c in range(4):
-                    _lib.call("mcgb_xy64_update_color", theta.cptr, rng.cptr, betas64.cptr, sig.cptr, R, L, r, c,
-                              1.0, 1.5, s)
-            if (start + k + 1) % EXCHANGE_INTERVAL == 0:
-                for r in range(R):
-                    _lib.call("mcgb_xy64_energy", theta.cptr, R, L, r, 1.0, energies.cptr, s)
-                _lib.call("mcgb_pt_exchange", energies.cptr, betas32.cptr, w2t.cptr, t2w.cptr, prng.cptr,
-                          counts.cptr, trips.cptr, R, ((start + k) // EXCHANGE_INTERVAL) & 1, start + k + 1, s)
-
-    sweeps(2, 0)
+    ladder = PlainXYLadder(L, temperatures(), seed, sigmas=sigma.astype(np.float64),
+                           exchange_interval=EXCHANGE_INTERVAL, initial_state=initial_angles(seed))
+    ladder.sweep(2)
     torch.cuda.synchronize()
     n = 20
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    sweeps(n, 2)
+    ladder.sweep(n)
     e1.record()
     torch.cuda.synchronize()
-    return R * L * L * n / (e0.elapsed_time(e1) * 1e6)
+    return N_TEMPS * L * L * n / (e0.elapsed_time(e1) * 1e6)
 
 
 def profile_windows(cluster_size=4, threads=1024):
@@ -447,10 +469,12 @@ def main():
         if line is not None and not args.no_cpu_baseline:
             cores = os.cpu_count() or 1
             v, dt = cpu_sample(cores, 500)
+            v1, dt1 = cpu_sample(1, 20)
             line["cpu_baseline"] = {"value": v, "unit": "updates/ns", "cores": cores, "kind": "port",
                                     "sample": f"500 sweeps of the same ladder with 50 exchanges, {cores} OpenMP "
                                               f"threads, {dt:.1f} s (the reference has no CPU sweep; its kernels "
-                                              f"restated in C)"}
+                                              f"restated in C)",
+                                    "one_core": {"value": v1, "sample": f"20 sweeps, 1 thread, {dt1:.1f} s"}}
     if line is not None:
         print(json.dumps(line), flush=True)
 

@@ -164,7 +164,8 @@ __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restric
 // Plain FP64 form: one replica per launch, float64 everywhere.
 __global__ void xy64_color_kernel(double *__restrict__ theta, ulonglong2 *__restrict__ rng,
                                   const double *__restrict__ betas, const double *__restrict__ sigmas,
-                                  int L, int r, int color, double J, double delta)
+                                  const int32_t *__restrict__ w2t, int L, int r, int color, double J,
+                                  double delta)
 {
     const double pi = 3.14159265358979323846, two_pi = 6.28318530717958647692;
     int rr, i, j;
@@ -174,6 +175,7 @@ __global__ void xy64_color_kernel(double *__restrict__ theta, ulonglong2 *__rest
     const double th = b[i * L + j];
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
     ulonglong2 st = rng[idx];
+    const int slot = w2t != nullptr ? w2t[r] : r;
     double proposed;
     if (sigmas == nullptr) {
         proposed = th + delta * (2.0 * xoro_uniform_f64(st) - 1.0);
@@ -183,7 +185,7 @@ __global__ void xy64_color_kernel(double *__restrict__ theta, ulonglong2 *__rest
         double u1 = xoro_uniform_f64(st);
         const double u2 = xoro_uniform_f64(st);
         if (u1 <= 0.0) u1 = 1.1102230246251565e-16;
-        proposed = th + sigmas[r] * (sqrt(-2.0 * log(u1)) * cos(two_pi * u2));
+        proposed = th + sigmas[slot] * (sqrt(-2.0 * log(u1)) * cos(two_pi * u2));
         proposed -= two_pi * floor((proposed + pi) / two_pi);
     }
     const double up = b[wrapi(i - 1, L) * L + j], down = b[wrapi(i + 1, L) * L + j];
@@ -194,7 +196,7 @@ __global__ void xy64_color_kernel(double *__restrict__ theta, ulonglong2 *__rest
     const double dE = e_new - e_old;
     const double v = xoro_uniform_f64(st);
     rng[idx] = st;
-    if (dE <= 0.0 || v < exp(-betas[r] * dE)) b[i * L + j] = proposed;
+    if (dE <= 0.0 || v < exp(-betas[slot] * dE)) b[i * L + j] = proposed;
 }
 
 // models/xy/measure.py:17-134.  NC = 1: energy only; NC = 5: all channels.
@@ -478,7 +480,8 @@ extern "C" int mcgb_xy_update_color_gauss(float *theta, void *rng, const float *
 }
 
 extern "C" int mcgb_xy64_update_color(double *theta, void *rng, const double *betas, const double *sigmas,
-                                      int R, int L, int r, int color, double J, double delta, void *stream)
+                                      const int32_t *w2t, int R, int L, int r, int color, double J, double delta,
+                                      void *stream)
 {
     if (int st = check_lattice("xy64_update_color", R, L)) return st;
     MCGB_REQUIRE(theta && rng && betas, "xy64_update_color: null pointer");
@@ -486,7 +489,7 @@ extern "C" int mcgb_xy64_update_color(double *theta, void *rng, const double *be
     MCGB_REQUIRE(color >= 0 && color < 4, "xy64_update_color: color must be 0..3");
     const int64_t n = (int64_t)(L / 2) * (L / 2);
     xy64_color_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
-        theta, static_cast<ulonglong2 *>(rng), betas, sigmas, L, r, color, J, delta);
+        theta, static_cast<ulonglong2 *>(rng), betas, sigmas, w2t, L, r, color, J, delta);
     return check_launch("xy64_color_kernel");
 }
 

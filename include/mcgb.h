@@ -84,10 +84,14 @@ int mcgb_xy_update_color_gauss(float *theta, void *rng, const float *betas,
                                const float *sigmas, int R, int L, int color, float J,
                                void *stream);
 /* Plain FP64 form: one lattice (replica r) per launch, float64 state,
- * float64 betas and sigmas, float64 uniforms; sigmas NULL = uniform delta. */
+ * float64 betas and sigmas, float64 uniforms; sigmas NULL = uniform delta.
+ * With w2t NULL, betas and sigmas are per walker; otherwise they are per
+ * temperature slot and walker r reads entry w2t[r] (a PT ladder whose
+ * exchanges permute w2t).  No reference counterpart: the float64 baseline
+ * the mixed-precision batch is compared with. */
 int mcgb_xy64_update_color(double *theta, void *rng, const double *betas,
-                           const double *sigmas, int R, int L, int r, int color, double J,
-                           double delta, void *stream);
+                           const double *sigmas, const int32_t *w2t, int R, int L, int r,
+                           int color, double J, double delta, void *stream);
 /* FP64 energy of one lattice (replica r) into out[r]. */
 int mcgb_xy64_energy(const double *theta, int R, int L, int r, double J, double *out,
                      void *stream);

@@ -99,7 +99,7 @@ def test_xy_plain_fp64_form_energy_and_moves():
     betas = device.to_device(np.zeros(R))
     for r in range(R):
         for c in range(4):
-            _lib.call("mcgb_xy64_update_color", d_th.cptr, rs.cptr, betas.cptr, None, R, L, r, c, 1.0, 1.5,
+            _lib.call("mcgb_xy64_update_color", d_th.cptr, rs.cptr, betas.cptr, None, None, R, L, r, c, 1.0, 1.5,
                       _lib.stream_handle())
     moved = d_th.copy_to_host()
     assert np.all(moved != th) and np.all(np.abs(moved) <= np.pi)
