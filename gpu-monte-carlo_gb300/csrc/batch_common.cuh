@@ -53,6 +53,59 @@ __device__ __forceinline__ void comp_add(float &sum, float &comp, float x)
     comp += e;
 }
 
+// A compensated float32 sum hi + lo (about 48 significant bits; exact for
+// integer terms).  The in-window sample reductions accumulate in these so
+// they run on the FP32 pipe: GB300's float64 pipe issues a small fraction of
+// the FP32 rate, and a per-site float64 accumulation dominated the cost of
+// taking a sample.
+struct FSum {
+    float hi, lo;
+    __device__ __forceinline__ FSum() : hi(0.0f), lo(0.0f) {}
+    __device__ __forceinline__ FSum &operator+=(float x)
+    {
+        comp_add(hi, lo, x);
+        return *this;
+    }
+    __device__ __forceinline__ void merge(float h, float l)
+    {
+        float s, e;
+        two_sum(hi, h, s, e);
+        hi = s;
+        lo += l + e;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Block reduction of NS compensated sums, all on the FP32 pipe; the result is
+// valid in thread 0.  `scratch` holds 32 * NS float2.
+template <int NS>
+__device__ __forceinline__ void block_fsum(FSum (&v)[NS], float2 *scratch)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NS; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            v[q].merge(__shfl_xor_sync(0xffffffffu, v[q].hi, off), __shfl_xor_sync(0xffffffffu, v[q].lo, off));
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) scratch[q * 32 + warp] = make_float2(v[q].hi, v[q].lo);
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            const float2 x = lane < nwarps ? scratch[q * 32 + lane] : make_float2(0.0f, 0.0f);
+            v[q].hi = x.x;
+            v[q].lo = x.y;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+                v[q].merge(__shfl_xor_sync(0xffffffffu, v[q].hi, off), __shfl_xor_sync(0xffffffffu, v[q].lo, off));
+        }
+    }
+}
+
 // The slot of the sample taken after sweep `sweep_no` (1-based, cumulative),
 // or -1 when no sample is due.  The buffer is a ring of n_slots samples: a
 // run longer than the buffer overwrites the oldest slots, so a replayed graph

@@ -163,15 +163,16 @@ struct KawamuraPolicy {
     }
     template <int C_>
     static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
-                                                   const float *, double *v)
+                                                   const float *, FSum *v)
     {
         const KawCell dn = MCGB_NBR(nb, kDown(C_));
+        const float third = 1.0f / 3.0f;
         v[1] += me.tau;
         v[2] += me.c * me.c - me.s * me.s;
         v[3] += 2.0f * me.c * me.s;
-        v[4] += (double)me.dx * me.dx - 1.0 / 3;
-        v[5] += (double)me.dy * me.dy - 1.0 / 3;
-        v[6] += (double)me.dz * me.dz - 1.0 / 3;
+        v[4] += fmaf(me.dx, me.dx, -third);
+        v[5] += fmaf(me.dy, me.dy, -third);
+        v[6] += fmaf(me.dz, me.dz, -third);
         v[7] += me.dx * me.dy;
         v[8] += me.dx * me.dz;
         v[9] += me.dy * me.dz;
@@ -416,12 +417,13 @@ struct He3Policy {
     }
     template <int C_>
     static __device__ __forceinline__ void measure(const Ctx &x, const Nbrs<Cell> &nb, const Cell &me, const float *,
-                                                   double *v)
+                                                   FSum *v)
     {
-        // models/he3/measure.py:33-60 (energy comes from the running cache).
+        // models/he3/measure.py:33-60 (energy comes from the running cache);
+        // per-site terms in float32, sums compensated.
         const He3Cell &Xp = MCGB_NBR(nb, kDown(C_));   // (i+1, j)
         const He3Cell &Yp = MCGB_NBR(nb, kRight(C_));  // (i, j+1)
-        const double K2 = 2.0 * (double)x.K;
+        const float K2 = 2.0f * x.K;
 #pragma unroll
         for (int mu = 0; mu < 3; ++mu) {
             const c32 X = me.z[2 * mu], Y = me.z[2 * mu + 1];
@@ -430,7 +432,7 @@ struct He3Policy {
             const float rd = norm2(X) + norm2(Y);
             v[1] += rd;
             if (mu == 2) v[9] += rd;
-            v[2] += 2.0 * (double)(conj(X) * Y).im;
+            v[2] += 2.0f * (conj(X) * Y).im;
             const c32 ph = X * X - Y * Y;
             v[3] += ph.re;
             v[4] += ph.im;
@@ -439,9 +441,9 @@ struct He3Policy {
             const c32 Cc = conj(c) + conj(b), Dd = 3.0f * conj(d) + conj(a);
             const c32 zy = Cc * ypx + Dd * ypy;
             v[5] += K2 * zx.im;
-            v[6] += K2 * (3.0 * norm2(xpx) + (double)norm2(xpy) - zx.re);
+            v[6] += K2 * ((3.0f * norm2(xpx) + norm2(xpy)) - zx.re);
             v[7] += K2 * zy.im;
-            v[8] += K2 * ((double)norm2(ypx) + 3.0 * norm2(ypy) - zy.re);
+            v[8] += K2 * ((norm2(ypx) + 3.0f * norm2(ypy)) - zy.re);
         }
     }
     template <int C_>

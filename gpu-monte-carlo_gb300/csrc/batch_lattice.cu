@@ -94,11 +94,11 @@ struct IsingPolicy {
     }
     template <int C_>
     static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
-                                                   const float *, double *v)
+                                                   const float *, FSum *v)
     {
         const int s = me;
-        v[0] += (double)(s * (MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kRight(C_))));
-        v[1] += (double)s;
+        v[0] += (float)(s * (MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kRight(C_))));
+        v[1] += (float)s;
     }
     template <int C_>
     static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
@@ -203,7 +203,7 @@ struct XYPolicy {
     }
     template <int C_>
     static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
-                                                   const float *, double *v)
+                                                   const float *, FSum *v)
     {
         const float2 dn = MCGB_NBR(nb, kDown(C_));
         v[1] += me.x;

@@ -39,7 +39,7 @@
 //   void store(const Args&, int64_t site, const Cell&, const float* own)
 //   Prop propose<c>(const Ctx&, const Cell&, const float* own, ulonglong2&)
 //   bool decide<c>(const Ctx&, Nbrs, Cell&, float* own, const Prop&, float& dE)
-//   void measure<c>(const Ctx&, Nbrs, const Cell&, const float* own, double* v)
+//   void measure<c>(const Ctx&, Nbrs, const Cell&, const float* own, FSum* v)
 //   void finish_sample(const Ctx&, double* v)  (turns kSums reduced sums, sum 0
 //        the energy, into the kChannels output channels, in place)
 // and two flags: kEnergyFromDelta (channel 0 = running energy + accepted
@@ -247,7 +247,7 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
 
 template <class M, int C_>
 __device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
-                                               const StripCtx &g, double *v)
+                                               const StripCtx &g, FSum *v)
 {
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
         const Site s = make_site(p, g.LP);
@@ -395,18 +395,19 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             const int slot = sample_slot(sweep0 + s + 1, cm.first_sample_sweep, cm.sample_interval, cm.n_slots);
             if (slot >= 0 && cm.samples != nullptr) {
                 cluster_wait();
-                double v[NS];
-#pragma unroll
-                for (int q = 0; q < NS; ++q) v[q] = 0.0;
-                v[0] = M::kEnergyFromDelta ? (double)dsum + (double)dcomp : 0.0;
+                FSum v[NS];
+                if (M::kEnergyFromDelta) {
+                    v[0].hi = dsum;
+                    v[0].lo = dcomp;
+                }
                 measure_colour<M, 0>(ctx, cells, own, g, v);
                 measure_colour<M, 1>(ctx, cells, own, g, v);
                 measure_colour<M, 2>(ctx, cells, own, g, v);
                 measure_colour<M, 3>(ctx, cells, own, g, v);
-                block_sum<NS>(v, scratch);
+                block_fsum<NS>(v, reinterpret_cast<float2 *>(scratch));
                 if (tid == 0) {
 #pragma unroll
-                    for (int q = 0; q < NS; ++q) red[q] = v[q];
+                    for (int q = 0; q < NS; ++q) red[q] = v[q].value();
                 }
                 cluster.sync();
                 if (rank == 0 && tid == 0) {
