@@ -10,7 +10,8 @@ every 10 sweeps.  One step = 100 sweeps of all 32 replicas
 
 Arms:
   default           the batched mixed-precision engine (mcgb.batch.LadderBatch),
-                    one window launch per 10 sweeps, CUDA-graph replay;
+                    one launch per 10 sweeps (sweeps, sample, exchange), CUDA-graph
+                    replay;
   --impl reference  the reference algorithm on the host cores: the C
                     restatement of its kernels (the reference has no CPU sweep
                     of its own), OpenMP over replicas, a bounded sample.
@@ -365,7 +366,8 @@ def run_mcgb(args, rank, world):
 
     # Plain FP64 form on the same ladder (one lattice per launch), bounded.
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
-    launches = args.steps * (SWEEPS_PER_STEP // EXCHANGE_INTERVAL) * 3
+    # One fused launch per window: sweeps, per-ladder exchange, clock tick.
+    launches = args.steps * (SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
 
     line = None
     if rank == 0:

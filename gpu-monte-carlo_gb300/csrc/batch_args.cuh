@@ -17,6 +17,7 @@ struct BatchArgs {
     float K, g_d, rho, mass;
     long long *counters;
     int n_replicas;
+    FusedExchange fx;  // enabled = 0: the window only
 };
 
 inline BatchArgs make_args(const mcgb_batch_window &w)
@@ -51,7 +52,49 @@ inline BatchArgs make_args(const mcgb_batch_window &w)
     a.mass = w.mass;
     a.counters = w.counters;
     a.n_replicas = w.n_replicas;
+    a.fx = FusedExchange{};
+    a.fx.enabled = 0;
     return a;
+}
+
+// Host-side checks shared by the exchange entry points.
+inline int check_exchange(const mcgb_batch_window &w, const mcgb_batch_pt &pt)
+{
+    MCGB_REQUIRE(w.energies && w.betas && w.w2t && w.clock && pt.t2w && pt.rng && pt.swap_counts && pt.trips &&
+                     pt.ladder_starts && pt.ladder_sizes,
+                 "batch_exchange: null pointer");
+    MCGB_REQUIRE(pt.n_ladders >= 1 && w.n_replicas >= 2 * pt.n_ladders,
+                 "batch_exchange: every ladder needs >= 2 replicas");
+    MCGB_REQUIRE(w.n_sweeps >= 0, "batch_exchange: n_sweeps must be >= 0");
+    MCGB_REQUIRE(w.staging == nullptr || (w.samples && pt.channels >= 1 && w.n_temps_total >= w.n_replicas),
+                 "batch_exchange: bad staging buffer");
+    return MCGB_OK;
+}
+
+inline ExchangeArgs make_exchange_args(const mcgb_batch_window &w, const mcgb_batch_pt &pt)
+{
+    ExchangeArgs x;
+    x.energies = w.energies;
+    x.betas = const_cast<float *>(w.betas);
+    x.w2t = const_cast<int32_t *>(w.w2t);
+    x.t2w = pt.t2w;
+    x.rng = static_cast<ulonglong2 *>(pt.rng);
+    x.counts = reinterpret_cast<long long *>(pt.swap_counts);
+    x.trips = reinterpret_cast<long long *>(pt.trips);
+    x.starts = pt.ladder_starts;
+    x.sizes = pt.ladder_sizes;
+    x.n_pairs_total = w.n_replicas - pt.n_ladders;
+    x.n_replicas = w.n_replicas;
+    x.clock = reinterpret_cast<const long long *>(w.clock);
+    x.window_sweeps = w.n_sweeps;
+    x.samples = w.samples;
+    x.staging = w.staging;
+    x.channels = pt.channels;
+    x.n_temps_total = w.n_temps_total;
+    x.n_slots = w.n_slots;
+    x.sample_interval = w.sample_interval;
+    x.first_sample_sweep = w.first_sample_sweep;
+    return x;
 }
 
 // Validate the table against the cluster shape.  Returns a negative status

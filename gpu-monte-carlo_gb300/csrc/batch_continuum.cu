@@ -574,11 +574,12 @@ int continuum_launch(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_
     return launch_window<M, 2>(a, w, s, name);
 }
 
-int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s)
+int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx)
 {
     if (int st = validate_window(w)) return st;
     MCGB_REQUIRE(model != MCGB_MODEL_KAWAMURA || w.aux != nullptr, "Kawamura window: null (cos, sin) cache");
-    const BatchArgs a = make_args(w);
+    BatchArgs a = make_args(w);
+    if (fx != nullptr) a.fx = *fx;
     switch (model) {
     case MCGB_MODEL_KAWAMURA: return continuum_launch<KawamuraPolicy>(a, w, s, "kawamura window");
     case MCGB_MODEL_HE3: return continuum_launch<He3Policy<false>>(a, w, s, "he3 window");

@@ -281,11 +281,12 @@ int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s)
     return check_launch("refresh_aux_kernel");
 }
 
-int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s)
+int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx)
 {
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w.aux != nullptr, "XY window: null (cos, sin) cache");
     if (int st = validate_window(w)) return st;
-    const BatchArgs a = make_args(w);
+    BatchArgs a = make_args(w);
+    if (fx != nullptr) a.fx = *fx;
     if (model == MCGB_MODEL_ISING)
         return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, s, "ising window")
                                : launch_window<IsingPolicy, 2>(a, w, s, "ising window");

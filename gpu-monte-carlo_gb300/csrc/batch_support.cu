@@ -4,12 +4,12 @@
 
 namespace mcgb {
 
-int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s);
+int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx = nullptr);
 int64_t lattice_smem(int model, int max_L, int C);
 int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out);
 int lattice_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s);
 int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s);
-int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s);
+int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx = nullptr);
 int64_t continuum_smem(int model, int max_L, int C);
 int continuum_max_clusters(int model, int C, int threads, size_t smem, int *out);
 int continuum_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s);
@@ -33,94 +33,8 @@ __global__ void permute_kernel(const W *__restrict__ src, W *__restrict__ dst, i
     for (int q = 0; q < words; ++q) dst[to * words + q] = src[from * words + q];
 }
 
-// One block per ladder: core/parallel_tempering.py:35-91 on ladder-local
-// indices.  Replicas of ladder l are [start, start + n); its exchange streams
-// and swap counters are at pair offset start - l.
-struct ExchangeArgs {
-    const double *energies;
-    float *betas;
-    int32_t *w2t, *t2w;
-    ulonglong2 *rng;
-    long long *counts, *trips;
-    const int32_t *starts, *sizes;
-    int n_pairs_total, n_replicas;
-    const long long *clock;
-    int window_sweeps;
-    // deferred window-end sample
-    double *samples;
-    const double *staging;
-    int channels, n_temps_total, n_slots, sample_interval;
-    long long first_sample_sweep;
-};
-
-__global__ void batch_exchange_kernel(const ExchangeArgs x)
-{
-    const int l = blockIdx.x;
-    const int start = x.starts[l], R = x.sizes[l];
-    const long long sweep = x.clock[0] + x.window_sweeps;
-    const int parity = R > 2 ? (int)(x.clock[1] & 1) : 0;
-    const int poff = start - l;
-    const double *E = x.energies + start;
-    float *B = x.betas + start;
-    int32_t *W2T = x.w2t + start, *T2W = x.t2w + start;
-    long long *attempts = x.counts + poff, *accepted = x.counts + x.n_pairs_total + poff,
-              *nonfinite = x.counts + 2 * x.n_pairs_total + poff;
-    for (int left = parity + 2 * (int)threadIdx.x; left < R - 1; left += 2 * blockDim.x) {
-        const int right = left + 1;
-        const int a = T2W[left], b = T2W[right];
-        const double ea = E[a], eb = E[b];
-        attempts[left] += 1;
-        if (!isfinite(ea) || !isfinite(eb)) {
-            nonfinite[left] += 1;
-            continue;
-        }
-        const double log_ratio = ((double)B[a] - (double)B[b]) * (ea - eb);
-        ulonglong2 st = x.rng[poff + left];
-        const double u = xoro_uniform_f64(st);
-        x.rng[poff + left] = st;
-        if (log_ratio >= 0.0 || u == 0.0 || log(u) < log_ratio) {
-            T2W[left] = b;
-            T2W[right] = a;
-            W2T[a] = right;
-            W2T[b] = left;
-            const float ba = B[a];
-            B[a] = B[b];
-            B[b] = ba;
-            accepted[left] += 1;
-        }
-    }
-    __syncthreads();
-    const int n = x.n_replicas;
-    long long *origin = x.trips + start, *visited = x.trips + n + start, *sweep0 = x.trips + 2 * n + start,
-              *ntrips = x.trips + 3 * n + start, *tsweeps = x.trips + 4 * n + start;
-    for (int wk = threadIdx.x; wk < R; wk += blockDim.x) {
-        const int t = W2T[wk];
-        if (t != 0 && t != R - 1) continue;
-        const long long o = origin[wk];
-        if (o < 0) {
-            origin[wk] = t;
-            sweep0[wk] = sweep;
-        } else if (t != o) {
-            visited[wk] = 1;
-        } else if (visited[wk]) {
-            ntrips[wk] += 1;
-            tsweeps[wk] += sweep - sweep0[wk];
-            sweep0[wk] = sweep;
-            visited[wk] = 0;
-        }
-    }
-    if (x.staging != nullptr && x.samples != nullptr) {
-        const int slot = sample_slot(sweep, x.first_sample_sweep, x.sample_interval, x.n_slots);
-        if (slot >= 0) {
-            for (int wk = threadIdx.x; wk < R; wk += blockDim.x) {
-                const int dst = start + W2T[wk];
-                for (int q = 0; q < x.channels; ++q)
-                    x.samples[((size_t)slot * x.channels + q) * x.n_temps_total + dst] =
-                        x.staging[(size_t)q * n + start + wk];
-            }
-        }
-    }
-}
+// One block per ladder.
+__global__ void batch_exchange_kernel(const ExchangeArgs x) { exchange_ladder(x, blockIdx.x); }
 
 __global__ void clock_tick_kernel(long long *clock, int n_sweeps, int exchanged)
 {
@@ -234,37 +148,27 @@ extern "C" int mcgb_batch_permute(const void *src, void *dst, int64_t elem_bytes
 extern "C" int mcgb_batch_exchange(const mcgb_batch_window *w, const mcgb_batch_pt *pt, void *stream)
 {
     MCGB_REQUIRE(w && pt, "batch_exchange: null argument block");
-    MCGB_REQUIRE(w->energies && w->betas && w->w2t && w->clock && pt->t2w && pt->rng && pt->swap_counts &&
-                     pt->trips && pt->ladder_starts && pt->ladder_sizes,
-                 "batch_exchange: null pointer");
-    MCGB_REQUIRE(pt->n_ladders >= 1 && w->n_replicas >= 2 * pt->n_ladders,
-                 "batch_exchange: every ladder needs >= 2 replicas");
-    MCGB_REQUIRE(w->n_sweeps >= 0, "batch_exchange: n_sweeps must be >= 0");
-    MCGB_REQUIRE(w->staging == nullptr || (w->samples && pt->channels >= 1 && w->n_temps_total >= w->n_replicas),
-                 "batch_exchange: bad staging buffer");
-    ExchangeArgs x;
-    x.energies = w->energies;
-    x.betas = const_cast<float *>(w->betas);
-    x.w2t = const_cast<int32_t *>(w->w2t);
-    x.t2w = pt->t2w;
-    x.rng = static_cast<ulonglong2 *>(pt->rng);
-    x.counts = reinterpret_cast<long long *>(pt->swap_counts);
-    x.trips = reinterpret_cast<long long *>(pt->trips);
-    x.starts = pt->ladder_starts;
-    x.sizes = pt->ladder_sizes;
-    x.n_pairs_total = w->n_replicas - pt->n_ladders;
-    x.n_replicas = w->n_replicas;
-    x.clock = reinterpret_cast<const long long *>(w->clock);
-    x.window_sweeps = w->n_sweeps;
-    x.samples = w->samples;
-    x.staging = w->staging;
-    x.channels = pt->channels;
-    x.n_temps_total = w->n_temps_total;
-    x.n_slots = w->n_slots;
-    x.sample_interval = w->sample_interval;
-    x.first_sample_sweep = w->first_sample_sweep;
-    batch_exchange_kernel<<<pt->n_ladders, 128, 0, as_stream(stream)>>>(x);
+    if (int st = check_exchange(*w, *pt)) return st;
+    batch_exchange_kernel<<<pt->n_ladders, 128, 0, as_stream(stream)>>>(make_exchange_args(*w, *pt));
     return check_launch("batch_exchange_kernel");
+}
+
+extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
+                                          int32_t *sync, void *stream)
+{
+    MCGB_REQUIRE(known_model(model), "unknown model %d", model);
+    MCGB_REQUIRE(w && pt, "window_exchange: null argument block");
+    MCGB_REQUIRE(sync != nullptr, "window_exchange: null sync counters");
+    if (int st = check_exchange(*w, *pt)) return st;
+    if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
+    if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
+    FusedExchange fx;
+    fx.ex = make_exchange_args(*w, *pt);
+    fx.ladder_done = sync;
+    fx.launch_done = sync + pt->n_ladders;
+    fx.enabled = 1;
+    return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
+                             : continuum_window(model, *w, as_stream(stream), &fx);
 }
 
 extern "C" int mcgb_batch_clock_tick(int64_t *clock, int n_sweeps, int exchanged, void *stream)

@@ -10,8 +10,13 @@
 // barrier, colour 3, barrier -- the visit order of four sequential colour
 // launches, since every site draws from its own stream.  Models whose sites
 // couple colours 1 and 2 (He3's diagonal gradient cells) set kSplitMiddle and
-// get a barrier between them.  Samples due inside the window are reduced
-// over the cluster and written in temperature order.
+// get a barrier between them.  A sample due after a sweep is measured by
+// every CTA, reduced over the CTA in compensated float32 and pushed into
+// rank 0's shared memory before the barrier that ends the sweep; one warp of
+// rank 0 combines the partial sums after the next wait and writes the sample
+// in temperature order (or stages it for the exchange when it falls on the
+// window's last sweep).  With a FusedExchange the same launch also runs each
+// ladder's replica exchange and advances the device clock.
 //
 // Halo rows.  Each colour plane of a strip is stored with one halo row above
 // and one below, so every neighbour read is a local shared-memory load at a
@@ -49,6 +54,7 @@
 #pragma once
 
 #include "batch_common.cuh"
+#include "batch_exchange.cuh"
 
 namespace mcgb {
 
@@ -126,12 +132,13 @@ struct WindowCommon {
 };
 
 constexpr int kRedDoubles = 16;  // per-CTA cluster reduction slots
+constexpr int kMaxCluster = 16;  // CTAs per cluster (non-portable maximum)
 
 // Shared memory of a strip with npl plaquettes in rows of lp.
 template <class M>
 __host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp)
 {
-    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3)) +
+    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * M::kSums) +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
            (size_t)4 * npl * sizeof(float) * M::kOwnFloats;
 }
@@ -257,6 +264,72 @@ __device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, typen
     }
 }
 
+// A sample's first half, out of line (it runs once per sample interval and
+// would otherwise crowd the sweep loop's instruction cache): measure the
+// strip, reduce over the CTA, push the partial sums into rank 0's `parts`.
+// The caller arrives at the cluster barrier afterwards, which publishes them.
+template <class M>
+__device__ __noinline__ void push_sample(const typename M::Ctx ctx, typename M::Cell *cells, float *own,
+                                         const StripCtx g, float dsum, float dcomp, float2 *scratch, float2 *parts,
+                                         int rank)
+{
+    constexpr int NS = M::kSums;
+    FSum v[NS];
+    if (M::kEnergyFromDelta) {
+        v[0].hi = dsum;
+        v[0].lo = dcomp;
+    }
+    measure_colour<M, 0>(ctx, cells, own, g, v);
+    measure_colour<M, 1>(ctx, cells, own, g, v);
+    measure_colour<M, 2>(ctx, cells, own, g, v);
+    measure_colour<M, 3>(ctx, cells, own, g, v);
+    block_fsum<NS>(v, scratch);
+    if (threadIdx.x == 0) {
+        float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NS;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
+    }
+}
+
+// Warp 0 of the cluster's rank-0 CTA turns the C partial sums of a sample
+// (pushed into its `parts` before the barrier that ended the sweep) into the
+// sample: lane q merges channel q over the CTAs in rank order, lane 0
+// finishes the sample and writes it to the staging row (pend == -2, a sample
+// on the window's last sweep, scattered by the exchange) or the ring slot.
+template <class M>
+__device__ __noinline__ void combine_sample(const typename M::Ctx ctx, const WindowCommon &cm, const float2 *parts,
+                                            double *red, int C, int pend, int r, int tslot, float e_hi0,
+                                            float e_lo0, int n_replicas)
+{
+    constexpr int NS = M::kSums, NC = M::kChannels;
+    const int lane = threadIdx.x;
+    if (lane < NS) {
+        FSum f;
+        for (int k = 0; k < C; ++k) {
+            const float2 q = parts[k * NS + lane];
+            f.merge(q.x, q.y);
+        }
+        red[lane] = f.value();
+    }
+    __syncwarp();
+    if (lane == 0) {
+        double tot[NS];
+#pragma unroll
+        for (int q = 0; q < NS; ++q) tot[q] = red[q];
+        if (M::kEnergyFromDelta) tot[0] += (double)e_hi0 + (double)e_lo0;
+        M::finish_sample(ctx, tot);
+        if (pend == -2) {
+#pragma unroll
+            for (int q = 0; q < NC; ++q) cm.staging[(size_t)q * n_replicas + r] = tot[q];
+        } else {
+            double *out = cm.samples + (size_t)pend * NC * cm.n_temps_total + tslot;
+#pragma unroll
+            for (int q = 0; q < NC; ++q) out[(size_t)q * cm.n_temps_total] = tot[q];
+        }
+    }
+    __syncwarp();
+}
+
 template <class M, int C_>
 __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
                                               const StripCtx &g, double &e)
@@ -272,6 +345,41 @@ __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typena
 // Threads per block the NPMAX variant is compiled for: NPMAX streams of four
 // colours live in registers (16 registers per plaquette); policies with large
 // cells cap it with kMaxThreads.
+// Fused exchange, run by the rank-0 CTA of a cluster after it finished
+// replica `rep`: the CTA that completes the ladder's last replica runs the
+// ladder's exchange (the classic last-block pattern: every finisher fences
+// its energies and staged sample, then counts; no thread waits on another).
+__device__ __forceinline__ void ladder_finished(const FusedExchange &fx, const mcgb_replica &rep)
+{
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(fx.ladder_done + rep.ladder, 1) == rep.n_temps - 1;
+        if (last) {
+            fx.ladder_done[rep.ladder] = 0;  // every replica of the ladder has counted
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    if (last) exchange_ladder(fx.ex, rep.ladder);
+}
+
+// After a cluster's whole work list (thread 0 of its rank-0 CTA): the last
+// cluster to finish advances the device clock, after every ladder's exchange
+// has read it, and resets the launch counter.
+__device__ __forceinline__ void launch_finished(const FusedExchange &fx, const WindowCommon &cm, int n_clusters)
+{
+    __threadfence();
+    if (atomicAdd(fx.launch_done, 1) == n_clusters - 1) {
+        __threadfence();
+        long long *clock = const_cast<long long *>(cm.clock);
+        clock[0] += cm.n_sweeps;
+        clock[1] += 1;
+        *fx.launch_done = 0;
+        __threadfence();
+    }
+}
+
 template <class M, int NPMAX>
 constexpr int window_max_threads()
 {
@@ -282,9 +390,8 @@ template <class M, int NPMAX>
 __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kernel(const typename M::Args a)
 {
     using Cell = typename M::Cell;
-    constexpr int NC = M::kChannels;  // output channels
-    constexpr int NS = M::kSums;      // reduced sums (>= NC)
-    static_assert(NS + 3 <= kRedDoubles, "too many reduced sums");
+    constexpr int NS = M::kSums;  // reduced sums (>= the kChannels output channels)
+    static_assert(NS + 3 <= kRedDoubles && NS <= 32, "too many reduced sums");
     constexpr int NK = NPMAX > 0 ? NPMAX : 1;
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
@@ -295,7 +402,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     extern __shared__ __align__(16) unsigned char smem[];
     double *red = reinterpret_cast<double *>(smem);  // kRedDoubles
     double *scratch = red + kRedDoubles;               // 32 * (NS + 3)
-    Cell *cells = reinterpret_cast<Cell *>(scratch + 32 * (NS + 3));
+    float2 *parts = reinterpret_cast<float2 *>(scratch + 32 * (NS + 3));  // [kMaxCluster][NS], rank 0's used
+    Cell *cells = reinterpret_cast<Cell *>(parts + kMaxCluster * NS);
 
     const WindowCommon &cm = a.c;
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
@@ -352,6 +460,15 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
 
         float dsum = 0.0f, dcomp = 0.0f;
         int nacc = 0;
+        // A sample whose partial sums wait in rank 0's `parts`: -1 none, -2
+        // the staged window-end sample, else its ring slot.
+        int pend = -1;
+#define MCGB_COMBINE_PENDING()                                                                              \
+    if (pend != -1) {                                                                                       \
+        if (rank == 0 && tid < 32)                                                                          \
+            combine_sample<M>(ctx, cm, parts, red, C, pend, r, tslot, e_hi0, e_lo0, a.n_replicas);          \
+        pend = -1;                                                                                          \
+    }
         typename M::Prop pa[NK], pb[NK];
         for (int s = 0; s < cm.n_sweeps; ++s) {
             if (regs) {
@@ -359,6 +476,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 // follows the previous phase and not yet waited.
                 propose_pass<M, NK, 0>(ctx, cells, own, g, sites, st, pa);
                 cluster_wait();
+                MCGB_COMBINE_PENDING()
                 decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
                 cluster_arrive();
                 propose_pass<M, NK, 1>(ctx, cells, own, g, sites, st, pa);
@@ -377,6 +495,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 cluster_arrive();
             } else {
                 cluster_wait();
+                MCGB_COMBINE_PENDING()
                 global_rng_pass<M, 0>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
                 cluster_arrive();
                 cluster_wait();
@@ -394,47 +513,17 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
 
             const int slot = sample_slot(sweep0 + s + 1, cm.first_sample_sweep, cm.sample_interval, cm.n_slots);
             if (slot >= 0 && cm.samples != nullptr) {
+                // Measure the strip, reduce over the CTA, push the partial
+                // sums into rank 0 ahead of the barrier that ends this phase.
                 cluster_wait();
-                FSum v[NS];
-                if (M::kEnergyFromDelta) {
-                    v[0].hi = dsum;
-                    v[0].lo = dcomp;
-                }
-                measure_colour<M, 0>(ctx, cells, own, g, v);
-                measure_colour<M, 1>(ctx, cells, own, g, v);
-                measure_colour<M, 2>(ctx, cells, own, g, v);
-                measure_colour<M, 3>(ctx, cells, own, g, v);
-                block_fsum<NS>(v, reinterpret_cast<float2 *>(scratch));
-                if (tid == 0) {
-#pragma unroll
-                    for (int q = 0; q < NS; ++q) red[q] = v[q].value();
-                }
-                cluster.sync();
-                if (rank == 0 && tid == 0) {
-                    double tot[NS];
-#pragma unroll
-                    for (int q = 0; q < NS; ++q) tot[q] = 0.0;
-                    for (int k = 0; k < C; ++k) {
-                        const double *rr = cluster.map_shared_rank(red, k);
-#pragma unroll
-                        for (int q = 0; q < NS; ++q) tot[q] += rr[q];
-                    }
-                    if (M::kEnergyFromDelta) tot[0] += (double)e_hi0 + (double)e_lo0;
-                    M::finish_sample(ctx, tot);
-                    if (cm.staging != nullptr && s + 1 == cm.n_sweeps) {
-                        // The exchange after this window scatters it with the new map.
-#pragma unroll
-                        for (int q = 0; q < NC; ++q) cm.staging[(size_t)q * a.n_replicas + r] = tot[q];
-                    } else {
-                        double *out = cm.samples + (size_t)slot * NC * cm.n_temps_total + tslot;
-#pragma unroll
-                        for (int q = 0; q < NC; ++q) out[(size_t)q * cm.n_temps_total] = tot[q];
-                    }
-                }
+                push_sample<M>(ctx, cells, own, g, dsum, dcomp, reinterpret_cast<float2 *>(scratch), parts, rank);
+                pend = (cm.staging != nullptr && s + 1 == cm.n_sweeps) ? -2 : slot;
                 cluster_arrive();
             }
         }
         cluster_wait();
+        MCGB_COMBINE_PENDING()
+#undef MCGB_COMBINE_PENDING
 
         // Window epilogue: energy and acceptance bookkeeping, write back.
         double v2[3] = {(double)dsum + (double)dcomp, (double)nacc, 0.0};
@@ -495,7 +584,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             cm.accepted[r] += (long long)na;
         }
         cluster.sync();
+        if (a.fx.enabled && rank == 0) ladder_finished(a.fx, rep);
     }
+    if (a.fx.enabled && rank == 0 && tid == 0) launch_finished(a.fx, cm, (int)(gridDim.x / C));
 }
 
 }  // namespace mcgb

@@ -240,6 +240,8 @@ class LadderBatch:
                 pair_rng[po:po + n - 1].raw().copy_(sub.raw())
             self.pair_rng = pair_rng
             self.swap_counts = device_zeros((3, n_pairs), np.int64)
+            # Completion counters of the fused window + exchange launch.
+            self.sync = device_zeros(n_l + 1, np.int32)
             trips = np.zeros((5, self.R), np.int64)
             trips[0] = -1
             trips[2] = -1
@@ -432,13 +434,22 @@ class LadderBatch:
         s = _lib.stream_handle()
         w = self._window(n_sweeps, staging=exchange)
         self._keep = w
+        if exchange and not tune:
+            # Window, per-ladder exchanges and clock tick in one launch.
+            p = self._pt()
+            self._keep_pt = p
+            _lib.call("mcgb_batch_window_exchange", self.model_id, ctypes.byref(w), ctypes.byref(p),
+                      self.sync.cptr, s)
+            return
         _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
+        if tune:
+            # The window's acceptance belongs to the temperatures it ran at:
+            # tune before the exchange moves replicas.
+            _lib.call("mcgb_batch_tune_sigma", self.sigma_t.cptr, self.accepted.cptr, self.accepted_prev.cptr,
+                      self.w2t.cptr, self.table.cptr, self.R, int(n_sweeps), 0.5, 2.0, 0.02, 2 * np.pi, s)
         if exchange:
             p = self._pt()
             _lib.call("mcgb_batch_exchange", ctypes.byref(w), ctypes.byref(p), s)
-        if tune:
-            _lib.call("mcgb_batch_tune_sigma", self.sigma_t.cptr, self.accepted.cptr, self.accepted_prev.cptr,
-                      self.w2t.cptr, self.table.cptr, self.R, int(n_sweeps), 0.5, 2.0, 0.02, 2 * np.pi, s)
         _lib.call("mcgb_batch_clock_tick", self.clock.cptr, int(n_sweeps), int(bool(exchange)), s)
 
     def _schedule(self, n_sweeps):

@@ -292,6 +292,16 @@ int mcgb_batch_exchange(const mcgb_batch_window *w, const mcgb_batch_pt *pt, voi
  * capture.  The caller ticks the clock as with the two separate calls. */
 int mcgb_batch_window_exchange_noalloc(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                        void *stream);
+/* No counterpart in the reference (it launches four colour kernels per sweep
+ * and one exchange kernel per round, core/parallel_tempering.py:245-269).
+ * mcgb_batch_window_run, mcgb_batch_exchange and
+ * mcgb_batch_clock_tick(clock, n_sweeps, 1) in ONE launch: the CTA that
+ * finishes the last replica of a ladder runs that ladder's exchange, and the
+ * last cluster to finish advances the clock.  `sync` is n_ladders + 1 int32
+ * counters, zero before the first call; every call leaves them zero.  Calls
+ * sharing a `sync` array must not overlap on the GPU. */
+int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
+                               int32_t *sync, void *stream);
 /* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
  * a captured graph of windows and exchanges can be replayed. */
 int mcgb_batch_clock_tick(int64_t *clock, int n_sweeps, int exchanged, void *stream);
