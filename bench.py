@@ -146,8 +146,9 @@ class ClockSampler:
 
 
 def cpu_sample(n_threads, sweeps, seed=7):
-    """Time the oracle (the reference algorithm restated in C) on the host
-    cores for `sweeps` sweeps of the ladder with exchanges; updates/ns."""
+    """Time the oracle (the reference algorithm restated in C: uniform
+    delta = 1.5 proposals, models/xy/update.py:6-54) on the host cores for
+    `sweeps` sweeps of the ladder with exchanges and samples; updates/ns."""
     import oracle
 
     temps = temperatures()
@@ -155,7 +156,6 @@ def cpu_sample(n_threads, sweeps, seed=7):
     theta = initial_angles(seed)
     rng = oracle.rng_states(R * L * L, seed)
     betas = (1.0 / temps).astype(np.float32)
-    sigmas = np.full(R, 0.93, np.float32)
     w2t = np.arange(R, dtype=np.int32)
     t2w = np.arange(R, dtype=np.int32)
     pair_rng = oracle.rng_states(R - 1, seed + 1)
@@ -165,8 +165,7 @@ def cpu_sample(n_threads, sweeps, seed=7):
     t0 = time.perf_counter()
     while done < sweeps:
         n = min(EXCHANGE_INTERVAL, sweeps - done)
-        oracle.xy_sweeps(theta, rng, betas, np.float32(1.0), np.float32(1.5), n,
-                         sigmas=sigmas[w2t], n_threads=n_threads)
+        oracle.xy_sweeps(theta, rng, betas, np.float32(1.0), np.float32(1.5), n, n_threads=n_threads)
         done += n
         if n == EXCHANGE_INTERVAL:
             e = oracle.xy_energy(theta, np.float32(1.0))

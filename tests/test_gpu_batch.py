@@ -320,3 +320,26 @@ def test_streams_in_global_memory_path_is_bit_exact():
     for _ in range(12):
         rt.sweep()
     np.testing.assert_array_equal(b.ladder_state(0), rt.snapshot())
+
+
+def test_simulated_ladders_save_load_and_summarise(tmp_path):
+    """LadderBatch.simulate -> run file (reference format) -> PT summary."""
+    from mcgb import ladder, pt_analysis, runs
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    ladders = ladder.ragged_ladders([8, 16], 2.0, 2.6, 6, Tc=2.269, tc_window=0.2, tc_fraction=0.5)
+    b = LadderBatch(IsingModel(), ladders, exchange_interval=5)
+    out = runs.runs_by_size(b.simulate(thermalization_sweeps=50, measurement_sweeps=200, sample_interval=10))
+    runs.save_runs(tmp_path / "fss.npz", out)
+    back = runs.load_runs(tmp_path / "fss.npz")
+    assert sorted(back) == [8, 16]
+    for L in (8, 16):
+        for name, values in out[L]["samples"].items():
+            np.testing.assert_array_equal(back[L]["samples"][name], values)
+        assert back[L]["samples"]["energy"].shape == (20, 6)
+    s = pt_analysis.pt_summary(back)
+    for L in (8, 16):
+        # 250 sweeps, an exchange every 5: 50 rounds of 3 and 2 pairs alternately.
+        assert sum(s[L]["attempts"]) == 25 * 3 + 25 * 2
+        assert 0 < s[L]["aggregate_acceptance"] <= 1
+        assert s[L]["temperatures"] == pytest.approx(list(ladders[0][1]))
