@@ -422,6 +422,211 @@ def plain_fp64_rate(batch, sigma, seed):
     return N_TEMPS * L * L * n / (e0.elapsed_time(e1) * 1e6)
 
 
+# ------------------------------------------------------------------ other workloads
+#
+# `--workload NAME` times another configuration of the study through the same
+# engine: a step is 100 sweeps of every replica with the configuration's
+# exchange and sampling schedule; the line keeps the default's keys (value,
+# e2e, roofline with the model's algorithmic bytes per update, clocks,
+# gpu_launches, cpu_baseline on a bounded sample of its first ladder).
+
+BYTES = {"ising": 34, "xy": 40, "kawamura": 72, "he3": 128}  # state r+w + 32 B RNG stream per update
+
+
+def workload_spec(name):
+    """(model kind, ladders, exchange_interval, sample_interval, description)."""
+    fss = (16, 32, 64, 128, 256, 512)
+    if name == "ising-l64":
+        return ("ising", [(64, [T]) for T in (1.5, 2.269, 3.0)], None, 1,
+                "Ising L=64 at T in {1.5, 2.269, 3.0}, single-temperature runs, E/N and |m| every sweep")
+    if name == "kawamura-l96x64":
+        return ("kawamura", [(96, np.linspace(0.65, 0.80, 48))] * 64, 10, 10,
+                "Kawamura L=96, 64 ladders x 48 temperatures linear in [0.65, 0.80] (3072 replicas), "
+                "reference proposals, exchange and sample every 10")
+    if name == "he3-ragged":
+        return ("he3", [(Lh, np.geomspace(0.33, 0.47, 24)) for Lh in (32, 48, 64, 96, 128)], 10, 10,
+                "He3 (class defaults) ragged L in {32,48,64,96,128} x 24 temperatures geometric in "
+                "[0.33, 0.47], conditional-Gaussian sampler, exchange and sample every 10")
+    if name == "fss-ising":
+        return ("ising", [(Lf, np.geomspace(2.0, 2.5, 64)) for Lf in fss for _ in range(8)], 10, 10,
+                "Ising FSS L in {16..512} x 8 ladders x 64 temperatures geometric in [2.0, 2.5] (3072 replicas)")
+    if name == "fss-xy":
+        return ("xy", [(Lf, np.geomspace(0.78, 1.02, 64)) for Lf in fss for _ in range(8)], 10, 10,
+                "XY FSS L in {16..512} x 8 ladders x 64 temperatures geometric in [0.78, 1.02] (3072 "
+                "replicas), Gaussian MH")
+    raise ValueError(f"unknown workload {name}")
+
+
+def seeded_state(kind, L_, R, seed):
+    """Seeded initial states in the reference layout."""
+    r = np.random.default_rng(seed)
+    if kind == "ising":
+        return r.choice(np.array([-1, 1], np.int8), (R, L_, L_))
+    if kind == "xy":
+        return r.uniform(-np.pi, np.pi, (R, L_, L_)).astype(np.float32)
+    if kind == "kawamura":
+        st = np.zeros((R, L_, L_, 5), np.float32)
+        st[..., 0] = r.uniform(-np.pi, np.pi, (R, L_, L_))
+        st[..., 1] = r.choice([-1.0, 1.0], (R, L_, L_))
+        d = r.normal(size=(R, L_, L_, 3))
+        st[..., 2:] = d / np.linalg.norm(d, axis=-1, keepdims=True)
+        return st
+    a = 0.3 * np.sqrt(2)
+    return (r.uniform(-a, a, (R, L_, L_, 3, 2)) + 1j * r.uniform(-a, a, (R, L_, L_, 3, 2))).astype(np.complex64)
+
+
+def cpu_sample_model(kind, L_, T, state, seed, n_threads, sweeps):
+    """The oracle (reference kernels restated in C) on one ladder, no exchange."""
+    import oracle
+    R = len(T)
+    betas = (1.0 / np.asarray(T)).astype(np.float32)
+    st = state.copy()
+    rng = oracle.rng_states(R * L_ * L_, seed)
+    t0 = time.perf_counter()
+    if kind == "ising":
+        oracle.ising_sweeps(st, rng, betas, np.float32(1), sweeps, n_threads=n_threads)
+    elif kind == "xy":
+        oracle.xy_sweeps(st, rng, betas, np.float32(1), np.float32(1.5), sweeps, n_threads=n_threads)
+    elif kind == "kawamura":
+        oracle.kawamura_sweeps(st, rng, betas, np.float32(1), np.float32(1.5), sweeps, n_threads=n_threads)
+    else:
+        coeff = np.array([-0.5, 1.0, 1.0, 1.0, -1.0], np.float32)
+        oracle.he3_sweeps(st, rng, betas, coeff, np.float32(1), np.float32(0.15), np.float32(0), sweeps,
+                          n_threads=n_threads)
+    dt = time.perf_counter() - t0
+    return R * L_ * L_ * sweeps / (dt * 1e9), dt
+
+
+def run_workload(args, rank, world):
+    import ctypes
+
+    import torch
+
+    from mcgb import _lib
+    from mcgb.batch import LadderBatch
+    from mcgb.models.he3.model import He3Model
+    from mcgb.models.ising.model import IsingModel
+    from mcgb.models.kawamura.model import KawamuraModel
+    from mcgb.models.xy.model import XYModel
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    kind, ladders, ex, si, desc = workload_spec(args.workload)
+    seeds = [42 + L_ + 100003 * k + 1000 * rank for k, (L_, _) in enumerate(ladders)]
+    inits = [seeded_state(kind, L_, len(T), sd) for (L_, T), sd in zip(ladders, seeds)]
+    model = {"ising": IsingModel(), "xy": XYModel(J=1.0), "kawamura": KawamuraModel(), "he3": He3Model()}[kind]
+    batch = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
+                        proposal="gaussian" if kind == "xy" else "uniform", gaussian=kind == "he3",
+                        initial_states=inits)
+    batch.autotune()
+    tune = kind == "xy"
+    batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=tune)
+    batch.allocate_samples(batch.sweeps + si, si, (args.steps + 2) * SWEEPS_PER_STEP // si)
+    batch.run(SWEEPS_PER_STEP)
+    torch.cuda.synchronize()
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    n_sites = int(batch.n_sites)
+    updates_per_step = n_sites * SWEEPS_PER_STEP
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.run(SWEEPS_PER_STEP)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = max_over_ranks(np.sum(step_ms), dist, "cuda")
+    value = aggregate_rate(world, updates_per_step, args.steps, total_ms)
+
+    # The window kernel alone (one window of the schedule, samples on).
+    win = ex or 10
+    w = batch._window(win)
+    _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+    torch.cuda.synchronize()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for _ in range(10):
+        _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+    k1.record(stream)
+    torch.cuda.synchronize()
+    window_ms = k0.elapsed_time(k1) / 10
+    peak, peak_kind = load_peaks()
+    achieved = BYTES[kind] * n_sites * win / (window_ms * 1e-3) / 1e9
+
+    # End to end: state and streams up from pinned memory, 100 sweeps, state,
+    # streams and the step's samples back.
+    host, out = batch.pinned_state_buffers(), batch.pinned_state_buffers()
+    batch.download_state(host)
+    batch.allocate_samples(batch.sweeps + si, si, SWEEPS_PER_STEP // si)
+    out_samples = torch.empty(batch.samples.nbytes, dtype=torch.uint8, pin_memory=True)
+    e2e_ms = []
+    n_e2e = min(args.steps, 20)
+    for i in range(n_e2e + 1):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.upload_state(host)
+        batch.run(SWEEPS_PER_STEP)
+        batch.download_state(out)
+        out_samples.copy_(batch.samples.raw(), non_blocking=True)
+        e1.record(stream)
+        e1.synchronize()
+        if i > 0:
+            e2e_ms.append(e0.elapsed_time(e1))
+    e2e_value = aggregate_rate(world, updates_per_step, n_e2e, max_over_ranks(np.sum(e2e_ms), dist, "cuda"))
+    h2d = sum(t.numel() for t in host.values())
+    d2h = sum(t.numel() for t in out.values()) + out_samples.numel()
+    if rank != 0:
+        return None
+    windows_per_step = SWEEPS_PER_STEP // win
+    line = {
+        "metric": METRIC, "value": value, "unit": "updates/ns", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"ising": "int8+f32", "he3": "c64"}.get(kind, "f32"),
+        "data": "synthetic (seeded initial states, reference has no dataset)",
+        "config": {"workload": desc, "replicas_per_gpu": int(batch.R), "sites_per_sweep": n_sites,
+                   "sweeps_per_step": SWEEPS_PER_STEP, "exchange_interval": ex, "sample_interval": si,
+                   "cluster_size": batch.cluster_size, "threads": batch.threads,
+                   "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": f"independent ladders x{world}"},
+        "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": n_e2e},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": f"window_kernel ({kind})", "kernel_ms": window_ms,
+                     "bytes_per_update": BYTES[kind], "peak_source": peak_kind},
+        "clocks": clk,
+        "gpu_launches": args.steps * windows_per_step * (1 if ex else 2),
+    }
+    if not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        L0, T0 = ladders[0]
+        sweeps = {"ising": 200, "xy": 40, "kawamura": 10, "he3": 4}[kind]
+        used = min(cores, len(T0))  # the oracle parallelises over replicas
+        v, dt = cpu_sample_model(kind, L0, T0, inits[0], seeds[0], used, sweeps)
+        line["cpu_baseline"] = {"value": v, "unit": "updates/ns", "cores": used, "kind": "port",
+                                "sample": f"{sweeps} sweeps of the first ladder (L={L0}, {len(T0)} replicas), "
+                                          f"reference proposals, no exchange, {dt:.1f} s"}
+    return line
+
+
 def profile_windows(cluster_size=4, threads=1024):
     """Small fixed case for ncu: the bench ladder, 3 warm windows + 3 windows."""
     import ctypes
@@ -454,6 +659,9 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: set up the ladder, then launch 6 window kernels and exit")
     ap.add_argument("--profile-shape", default="4,1024", help="cluster_size,threads for --profile")
+    ap.add_argument("--workload", default="xy-pt-l128",
+                    choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "he3-ragged", "fss-ising", "fss-xy"],
+                    help="configuration to time (default: the XY PT ladder the metric is quoted on)")
     args = ap.parse_args()
     if args.profile:
         c, t = (int(x) for x in args.profile_shape.split(","))
@@ -465,6 +673,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.workload != "xy-pt-l128":
+        line = run_workload(args, rank, world)
     else:
         line = run_mcgb(args, rank, world)
         if line is not None and not args.no_cpu_baseline:
