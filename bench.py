@@ -627,21 +627,36 @@ def run_workload(args, rank, world):
     return line
 
 
-def profile_windows(cluster_size=4, threads=1024):
-    """Small fixed case for ncu: the bench ladder, 3 warm windows + 3 windows."""
+def profile_windows(cluster_size=4, threads=1024, workload="xy-pt-l128"):
+    """Small fixed case for ncu: the workload's batch, 3 warm windows + 3 windows."""
     import ctypes
 
     import torch
 
     from mcgb import _lib
     from mcgb.batch import LadderBatch
+    from mcgb.models.he3.model import He3Model
+    from mcgb.models.ising.model import IsingModel
+    from mcgb.models.kawamura.model import KawamuraModel
     from mcgb.models.xy.model import XYModel
 
-    seed = 42 + L
-    b = LadderBatch(XYModel(J=1.0), [(L, temperatures())], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
-                    proposal="gaussian", sigma0=0.93, cluster_size=cluster_size, threads=threads,
-                    initial_states=[initial_angles(seed)])
-    w = b._window(EXCHANGE_INTERVAL)
+    if workload == "xy-pt-l128":
+        seed = 42 + L
+        b = LadderBatch(XYModel(J=1.0), [(L, temperatures())], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
+                        proposal="gaussian", sigma0=0.93, cluster_size=cluster_size, threads=threads,
+                        initial_states=[initial_angles(seed)])
+        win = EXCHANGE_INTERVAL
+    else:
+        kind, ladders, ex, _, _ = workload_spec(workload)
+        seeds = [42 + L_ + 100003 * k for k, (L_, _) in enumerate(ladders)]
+        inits = [seeded_state(kind, L_, len(T), sd) for (L_, T), sd in zip(ladders, seeds)]
+        model = {"ising": IsingModel(), "xy": XYModel(J=1.0), "kawamura": KawamuraModel(),
+                 "he3": He3Model()}[kind]
+        b = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
+                        proposal="gaussian" if kind == "xy" else "uniform", gaussian=kind == "he3",
+                        cluster_size=cluster_size, threads=threads, initial_states=inits)
+        win = ex or 10
+    w = b._window(win)
     for _ in range(6):
         _lib.call("mcgb_batch_window_run", b.model_id, ctypes.byref(w), _lib.stream_handle())
     torch.cuda.synchronize()
@@ -665,7 +680,7 @@ def main():
     args = ap.parse_args()
     if args.profile:
         c, t = (int(x) for x in args.profile_shape.split(","))
-        profile_windows(c, t)
+        profile_windows(c, t, args.workload)
         return
     if args.warmup < 3:
         ap.error("warm-up must be at least 3 steps")
