@@ -154,8 +154,8 @@ struct XYPolicy {
         static_cast<float *>(a.state)[site] = own[0];
         a.aux[site] = cell;
     }
-    // Draws (in order): Gaussian u1, u2, accept v; uniform u, accept v.  The
-    // mixed form uses 23-bit uniforms (mcgb_fast_unit).
+    // Draws (in order): Gaussian (u1, u2) from one draw, accept v; uniform
+    // u, accept v.  The mixed form uses 23-bit uniforms (mcgb_fast_unit).
     template <int C_>
     static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &, const float *own, ulonglong2 &st)
     {
@@ -163,8 +163,9 @@ struct XYPolicy {
         const float t = own[0];
         Prop q;
         if (x.gauss) {
-            float u1 = mcgb_fast_unit(xoro_next(st));
-            const float u2 = mcgb_fast_unit(xoro_next(st));
+            const uint64_t bits = xoro_next(st);
+            float u1 = mcgb_fast_unit(bits);
+            const float u2 = mcgb_fast_unit_mid(bits);
             if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
             const float t2 = -2.0f * __logf(u1);
             // cos(2 pi u2) = -cos(2 pi u2 - pi), evaluated on [-pi, pi].

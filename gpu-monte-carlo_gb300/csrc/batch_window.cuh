@@ -206,7 +206,7 @@ __device__ __forceinline__ void propose_pass(const typename M::Ctx &ctx, const t
 template <class M, int NK, int C_>
 __device__ __forceinline__ void decide_pass(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
                                             const StripCtx &g, const Site (&sites)[NK],
-                                            const typename M::Prop (&prop)[NK], float &dsum, float &dcomp,
+                                            const typename M::Prop (&prop)[NK], float &dacc,
                                             int &nacc)
 {
 #pragma unroll
@@ -218,7 +218,7 @@ __device__ __forceinline__ void decide_pass(const typename M::Ctx &ctx, typename
             typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
             float dE;
             if (M::template decide<C_>(ctx, nb, me, own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, prop[k], dE)) {
-                comp_add(dsum, dcomp, dE);
+                dacc += dE;
                 ++nacc;
                 push_halo<C_>(cells, g, s, me);
             }
@@ -231,7 +231,7 @@ __device__ __forceinline__ void decide_pass(const typename M::Ctx &ctx, typename
 template <class M, int C_>
 __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const typename M::Ctx &ctx,
                                                 typename M::Cell *cells, float *own, const StripCtx &g,
-                                                int64_t base, int64_t gplane, float &dsum, float &dcomp, int &nacc)
+                                                int64_t base, int64_t gplane, float &dacc, int &nacc)
 {
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(a.c.rng);
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
@@ -245,7 +245,7 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
         float dE;
         if (M::template decide<C_>(ctx, nb, me, o, pr, dE)) {
-            comp_add(dsum, dcomp, dE);
+            dacc += dE;
             ++nacc;
             push_halo<C_>(cells, g, s, me);
         }
@@ -471,46 +471,50 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     }
         typename M::Prop pa[NK], pb[NK];
         for (int s = 0; s < cm.n_sweeps; ++s) {
+            // This sweep's accepted energy changes (at most a few terms per
+            // thread), folded into the compensated running sum once per sweep.
+            float dacc = 0.0f;
             if (regs) {
                 // Invariant: this thread has arrived at the barrier that
                 // follows the previous phase and not yet waited.
                 propose_pass<M, NK, 0>(ctx, cells, own, g, sites, st, pa);
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
-                decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
+                decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 cluster_arrive();
                 propose_pass<M, NK, 1>(ctx, cells, own, g, sites, st, pa);
                 propose_pass<M, NK, 2>(ctx, cells, own, g, sites, st, pb);
                 cluster_wait();
-                decide_pass<M, NK, 1>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
+                decide_pass<M, NK, 1>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 if (M::kSplitMiddle) {
                     cluster_arrive();
                     cluster_wait();
                 }
-                decide_pass<M, NK, 2>(ctx, cells, own, g, sites, pb, dsum, dcomp, nacc);
+                decide_pass<M, NK, 2>(ctx, cells, own, g, sites, pb, dacc, nacc);
                 cluster_arrive();
                 propose_pass<M, NK, 3>(ctx, cells, own, g, sites, st, pa);
                 cluster_wait();
-                decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dsum, dcomp, nacc);
+                decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 cluster_arrive();
             } else {
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
-                global_rng_pass<M, 0>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                global_rng_pass<M, 0>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 cluster_arrive();
                 cluster_wait();
-                global_rng_pass<M, 1>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                global_rng_pass<M, 1>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 if (M::kSplitMiddle) {
                     cluster_arrive();
                     cluster_wait();
                 }
-                global_rng_pass<M, 2>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                global_rng_pass<M, 2>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 cluster_arrive();
                 cluster_wait();
-                global_rng_pass<M, 3>(a, ctx, cells, own, g, base, gplane, dsum, dcomp, nacc);
+                global_rng_pass<M, 3>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 cluster_arrive();
             }
 
+            comp_add(dsum, dcomp, dacc);
             const int slot = sample_slot(sweep0 + s + 1, cm.first_sample_sweep, cm.sample_interval, cm.n_slots);
             if (slot >= 0 && cm.samples != nullptr) {
                 // Measure the strip, reduce over the CTA, push the partial

@@ -144,8 +144,10 @@ __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restric
         if (proposed >= pi) proposed -= two_pi;
         else if (proposed < -pi) proposed += two_pi;
     } else {
-        float u1 = xoro_uniform_f32(st);
-        const float u2 = xoro_uniform_f32(st);
+        // Two draws per visit: u1, u2 from bits 63..41 and 40..18 of one.
+        const uint64_t x = xoro_next(st);
+        float u1 = mcgb_fast_unit(x);
+        const float u2 = mcgb_fast_unit_mid(x);
         if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
         const float z = sqrtf(-2.0f * logf(u1)) * cosf(two_pi * u2);
         proposed = th + sigmas[r] * z;

@@ -128,3 +128,11 @@ MCGB_HD float mcgb_fast_unit(uint64_t x)
 {
     return mcgb_bits_to_float(0x3f800000u | (uint32_t)(x >> 41)) - 1.0f;
 }
+
+// The same from bits 40..18 of x, the next 23 bits below mcgb_fast_unit's:
+// one draw yields two independent 23-bit uniforms (both away from the
+// generator's weak lowest bits).
+MCGB_HD float mcgb_fast_unit_mid(uint64_t x)
+{
+    return mcgb_bits_to_float(0x3f800000u | ((uint32_t)(x >> 18) & 0x7fffffu)) - 1.0f;
+}

@@ -197,7 +197,9 @@ void orc_ising_measure(const int8_t *spins, int R, int L, float J,
 /* XY: models/xy/update.py:6-54, models/xy/measure.py:17-134                */
 /* The Gaussian-proposal variant is this project's extension (symmetric     */
 /* proposal theta + sigma*z, Box-Muller z, full wrap); it reuses the       */
-/* reference's acceptance rule and draw discipline (every draw is taken).   */
+/* reference's acceptance rule.  Two draws per visit: the Box-Muller pair  */
+/* u1, u2 are bits 63..41 and 40..18 of the first (23-bit uniforms), the   */
+/* acceptance uniform is the float32 uniform of the second.                */
 /* ------------------------------------------------------------------------ */
 
 static const float PI_F = 3.14159265358979323846f;
@@ -228,8 +230,9 @@ static void xy_color_replica(float *theta, uint64_t *rng, float beta, int r, int
                 if (proposed >= PI_F) proposed -= TWO_PI_F;
                 else if (proposed < -PI_F) proposed += TWO_PI_F;
             } else {
-                float u1 = orc_rng_uniform_f32(st);
-                float u2 = orc_rng_uniform_f32(st);
+                uint64_t x = orc_rng_next(st);
+                float u1 = (float)(x >> 41) * 0x1p-23f;
+                float u2 = (float)((x >> 18) & 0x7fffffu) * 0x1p-23f;
                 if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
                 float z = sqrtf(-2.0f * logf(u1)) * cosf(TWO_PI_F * u2);
                 proposed = t + sigma * z;
