@@ -335,8 +335,9 @@ def run_mcgb(args, rank, world):
     achieved = alg_bytes / (window_ms * 1e-3) / 1e9
 
     # End to end through the public API with host buffers: every step uploads
-    # the ladder's angles and RNG streams from pinned memory, runs 100 sweeps
-    # and reads back the angles, RNG streams and the step's samples.
+    # the chain state (angles, RNG streams, (cos, sin) cache, running
+    # energies) from pinned memory, runs 100 sweeps and reads back the chain
+    # state and the step's samples.
     host = batch.pinned_state_buffers()
     out = batch.pinned_state_buffers()
     n_s = SWEEPS_PER_STEP // SAMPLE_INTERVAL
@@ -570,8 +571,8 @@ def run_workload(args, rank, world):
     peak, peak_kind = load_peaks()
     achieved = BYTES[kind] * n_sites * win / (window_ms * 1e-3) / 1e9
 
-    # End to end: state and streams up from pinned memory, 100 sweeps, state,
-    # streams and the step's samples back.
+    # End to end: the chain state up from pinned memory, 100 sweeps, the
+    # chain state and the step's samples back.
     host, out = batch.pinned_state_buffers(), batch.pinned_state_buffers()
     batch.download_state(host)
     batch.allocate_samples(batch.sweeps + si, si, SWEEPS_PER_STEP // si)

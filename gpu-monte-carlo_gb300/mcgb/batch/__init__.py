@@ -523,24 +523,36 @@ class LadderBatch:
         self.exchange_rounds += 1
 
     # ------------------------------------------------------------ host I/O
-    def pinned_state_buffers(self):
-        """Pinned host byte buffers for the ladder state and RNG (engine layout)."""
-        import torch as _t
-        return {"state": _t.empty(self.state.nbytes, dtype=_t.uint8, pin_memory=True),
-                "rng": _t.empty(self.rng.nbytes, dtype=_t.uint8, pin_memory=True)}
+    def _host_fields(self):
+        fields = {"state": self.state, "rng": self.rng, "e_run": self.e_run}
+        if self.aux is not None:
+            fields["aux"] = self.aux
+        return fields
 
-    def upload_state(self, host):
-        """Asynchronous host-to-device copy of state and RNG (engine layout) from
-        pinned buffers, then the (cos, sin) cache and exact energies."""
-        self.state.raw().copy_(host["state"], non_blocking=True)
-        self.rng.raw().copy_(host["rng"], non_blocking=True)
-        self.refresh_aux()
-        self.recompute_energy()
+    def pinned_state_buffers(self):
+        """Pinned host byte buffers for the chain state in the engine layout:
+        spins/angles, RNG streams, the running energies and, for XY and
+        Kawamura, the (cos, sin) cache."""
+        import torch as _t
+        return {k: _t.empty(v.nbytes, dtype=_t.uint8, pin_memory=True) for k, v in self._host_fields().items()}
+
+    def upload_state(self, host, recompute=False):
+        """Asynchronous host-to-device copy from pinned buffers.  A buffer set
+        from download_state resumes the chain exactly; when it holds only
+        ``state`` and ``rng`` (or ``recompute`` is set), the (cos, sin) cache
+        and the exact energies are rebuilt on the device instead."""
+        for k, arr in self._host_fields().items():
+            if k in host:
+                arr.raw().copy_(host[k], non_blocking=True)
+        if recompute or "e_run" not in host or (self.aux is not None and "aux" not in host):
+            self.refresh_aux()
+            self.recompute_energy()
 
     def download_state(self, host):
-        """Asynchronous device-to-host copy of state and RNG into pinned buffers."""
-        host["state"].copy_(self.state.raw(), non_blocking=True)
-        host["rng"].copy_(self.rng.raw(), non_blocking=True)
+        """Asynchronous device-to-host copy of the chain state into pinned buffers."""
+        for k, arr in self._host_fields().items():
+            if k in host:
+                host[k].copy_(arr.raw(), non_blocking=True)
 
     def checkpoint(self):
         """Everything needed to resume the chain bit-exactly, as host arrays."""
