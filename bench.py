@@ -431,7 +431,7 @@ def plain_fp64_rate(batch, sigma, seed):
 # e2e, roofline with the model's algorithmic bytes per update, clocks,
 # gpu_launches, cpu_baseline on a bounded sample of its first ladder).
 
-BYTES = {"ising": 34, "xy": 40, "kawamura": 72, "he3": 128}  # state r+w + 32 B RNG stream per update
+BYTES = {"ising": 34, "xy": 40, "kawamura": 72, "kawamura-gauss": 72, "he3": 128}  # state r+w + 32 B RNG
 
 
 def workload_spec(name):
@@ -441,9 +441,13 @@ def workload_spec(name):
         return ("ising", [(64, [T]) for T in (1.5, 2.269, 3.0)], None, 1,
                 "Ising L=64 at T in {1.5, 2.269, 3.0}, single-temperature runs, E/N and |m| every sweep")
     if name == "kawamura-l96x64":
+        return ("kawamura-gauss", [(96, np.linspace(0.65, 0.80, 48))] * 64, 10, 10,
+                "Kawamura L=96, 64 ladders x 48 temperatures linear in [0.65, 0.80] (3072 replicas), "
+                "Gaussian MH (theta and d, widths tuned to ~50%), exchange and sample every 10")
+    if name == "kawamura-l96x64-reference-proposals":
         return ("kawamura", [(96, np.linspace(0.65, 0.80, 48))] * 64, 10, 10,
                 "Kawamura L=96, 64 ladders x 48 temperatures linear in [0.65, 0.80] (3072 replicas), "
-                "reference proposals, exchange and sample every 10")
+                "the reference's uniform/flip/sphere proposals, exchange and sample every 10")
     if name == "he3-ragged":
         return ("he3", [(Lh, np.geomspace(0.33, 0.47, 24)) for Lh in (32, 48, 64, 96, 128)], 10, 10,
                 "He3 (class defaults) ragged L in {32,48,64,96,128} x 24 temperatures geometric in "
@@ -461,6 +465,7 @@ def workload_spec(name):
 def seeded_state(kind, L_, R, seed):
     """Seeded initial states in the reference layout."""
     r = np.random.default_rng(seed)
+    kind = kind.split("-")[0]
     if kind == "ising":
         return r.choice(np.array([-1, 1], np.int8), (R, L_, L_))
     if kind == "xy":
@@ -477,8 +482,10 @@ def seeded_state(kind, L_, R, seed):
 
 
 def cpu_sample_model(kind, L_, T, state, seed, n_threads, sweeps):
-    """The oracle (reference kernels restated in C) on one ladder, no exchange."""
+    """The oracle (reference kernels restated in C, reference proposals) on
+    one ladder, no exchange."""
     import oracle
+    kind = kind.split("-")[0]
     R = len(T)
     betas = (1.0 / np.asarray(T)).astype(np.float32)
     st = state.copy()
@@ -519,12 +526,14 @@ def run_workload(args, rank, world):
     kind, ladders, ex, si, desc = workload_spec(args.workload)
     seeds = [42 + L_ + 100003 * k + 1000 * rank for k, (L_, _) in enumerate(ladders)]
     inits = [seeded_state(kind, L_, len(T), sd) for (L_, T), sd in zip(ladders, seeds)]
-    model = {"ising": IsingModel(), "xy": XYModel(J=1.0), "kawamura": KawamuraModel(), "he3": He3Model()}[kind]
+    gauss = kind in ("xy", "kawamura-gauss")
+    model = {"ising": IsingModel(), "xy": XYModel(J=1.0), "kawamura": KawamuraModel(),
+             "kawamura-gauss": KawamuraModel(), "he3": He3Model()}[kind]
     batch = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
-                        proposal="gaussian" if kind == "xy" else "uniform", gaussian=kind == "he3",
-                        initial_states=inits)
+                        proposal="gaussian" if gauss else "uniform", gaussian=kind == "he3",
+                        sigma0=0.5 if kind == "kawamura-gauss" else 1.0, initial_states=inits)
     batch.autotune()
-    tune = kind == "xy"
+    tune = gauss
     batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=tune)
     batch.allocate_samples(batch.sweeps + si, si, (args.steps + 2) * SWEEPS_PER_STEP // si)
     batch.run(SWEEPS_PER_STEP)
@@ -619,7 +628,7 @@ def run_workload(args, rank, world):
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         L0, T0 = ladders[0]
-        sweeps = {"ising": 200, "xy": 40, "kawamura": 10, "he3": 4}[kind]
+        sweeps = {"ising": 200, "xy": 40, "kawamura": 10, "kawamura-gauss": 10, "he3": 4}[kind]
         used = min(cores, len(T0))  # the oracle parallelises over replicas
         v, dt = cpu_sample_model(kind, L0, T0, inits[0], seeds[0], used, sweeps)
         line["cpu_baseline"] = {"value": v, "unit": "updates/ns", "cores": used, "kind": "port",
@@ -652,10 +661,10 @@ def profile_windows(cluster_size=4, threads=1024, workload="xy-pt-l128"):
         seeds = [42 + L_ + 100003 * k for k, (L_, _) in enumerate(ladders)]
         inits = [seeded_state(kind, L_, len(T), sd) for (L_, T), sd in zip(ladders, seeds)]
         model = {"ising": IsingModel(), "xy": XYModel(J=1.0), "kawamura": KawamuraModel(),
-                 "he3": He3Model()}[kind]
+                 "kawamura-gauss": KawamuraModel(), "he3": He3Model()}[kind]
         b = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
-                        proposal="gaussian" if kind == "xy" else "uniform", gaussian=kind == "he3",
-                        cluster_size=cluster_size, threads=threads, initial_states=inits)
+                        proposal="gaussian" if kind in ("xy", "kawamura-gauss") else "uniform",
+                        gaussian=kind == "he3", cluster_size=cluster_size, threads=threads, initial_states=inits)
         win = ex or 10
     w = b._window(win)
     for _ in range(6):
@@ -676,7 +685,8 @@ def main():
                     help="profiling driver: set up the ladder, then launch 6 window kernels and exit")
     ap.add_argument("--profile-shape", default="4,1024", help="cluster_size,threads for --profile")
     ap.add_argument("--workload", default="xy-pt-l128",
-                    choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "he3-ragged", "fss-ising", "fss-xy"],
+                    choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "kawamura-l96x64-reference-proposals",
+                             "he3-ragged", "fss-ising", "fss-xy"],
                     help="configuration to time (default: the XY PT ladder the metric is quoted on)")
     args = ap.parse_args()
     if args.profile:

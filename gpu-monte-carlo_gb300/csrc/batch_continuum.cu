@@ -35,6 +35,13 @@ struct KawCell {
     float c, s, tau, dx, dy, dz;
 };
 
+// kGauss: Gaussian proposals (this project's extension, no reference
+// counterpart): theta' = theta + sigma z0 (wrapped), d' = normalise(d + sigma g)
+// with g three standard normals -- symmetric, since its density depends only
+// on the angle between d and d' -- and the reference's tau flip.  Five draws
+// per visit: the normal pairs (z0, gx) and (gy, gz), each from bits 63..41
+// and 40..18 of one draw, then the three acceptance uniforms.
+template <bool kGauss>
 struct KawamuraPolicy {
     using Args = BatchArgs;
     using Cell = KawCell;
@@ -47,7 +54,7 @@ struct KawamuraPolicy {
     static constexpr bool kExactEnergy = false;
 
     struct Ctx {
-        float beta, J, delta;
+        float beta, J, delta, sigma;
     };
     struct Prop {
         float tp, cp, sp;  // theta proposal and its (cos, sin)
@@ -55,9 +62,20 @@ struct KawamuraPolicy {
         float v1, v2, v3;  // acceptance uniforms of the three sub-moves
     };
 
-    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
     {
-        return Ctx{a.c.betas[r], a.J, a.delta};
+        return Ctx{a.c.betas[r], a.J, a.delta, kGauss ? a.sigma_t[rep.ladder_start + a.c.w2t[r]] : 0.0f};
+    }
+    // A pair of standard normals from one draw (Box-Muller, fast intrinsics).
+    static __device__ __forceinline__ float2 normal_pair(uint64_t bits)
+    {
+        float u = mcgb_fast_unit(bits);
+        if (u <= 0.0f) u = 1.1102230246251565e-16f;
+        const float t = -2.0f * __logf(u);
+        const float rad = t * rsqrtf(t);
+        float sn, cs;
+        __sincosf(fmaf(kTwoPi, mcgb_fast_unit_mid(bits), -kPi), &sn, &cs);  // angle - pi
+        return make_float2(-rad * cs, -rad * sn);
     }
     static __device__ __forceinline__ void load(const Args &a, int64_t site, Cell &cell, float *own)
     {
@@ -77,9 +95,29 @@ struct KawamuraPolicy {
         a.aux[site] = make_float2(cell.c, cell.s);
     }
     template <int C_>
-    static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &, const float *own, ulonglong2 &st)
+    static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &me, const float *own, ulonglong2 &st)
     {
         Prop q;
+        if (kGauss) {
+            const float2 n0 = normal_pair(xoro_next(st));
+            const float2 n1 = normal_pair(xoro_next(st));
+            float tp = fmaf(x.sigma, n0.x, own[0]);
+            tp -= kTwoPi * floorf((tp + kPi) * (1.0f / kTwoPi));
+            if (tp >= kPi) tp -= kTwoPi;
+            if (tp < -kPi) tp += kTwoPi;
+            q.tp = tp;
+            __sincosf(tp, &q.sp, &q.cp);
+            q.v1 = mcgb_fast_unit(xoro_next(st));
+            q.v2 = mcgb_fast_unit(xoro_next(st));
+            const float gx = fmaf(x.sigma, n0.y, me.dx), gy = fmaf(x.sigma, n1.x, me.dy),
+                        gz = fmaf(x.sigma, n1.y, me.dz);
+            const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
+            q.x = gx * inv;
+            q.y = gy * inv;
+            q.z = gz * inv;
+            q.v3 = mcgb_fast_unit(xoro_next(st));
+            return q;
+        }
         float tp = own[0] + x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
         if (tp >= kPi) tp -= kTwoPi;
         else if (tp < -kPi) tp += kTwoPi;
@@ -520,7 +558,7 @@ __global__ void batch_energy64_continuum(int model, const void *state, const mcg
     for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
         const int i = k / L, j = k - i * L;
         const int id = i + 1 == L ? 0 : i + 1, jr = j + 1 == L ? 0 : j + 1;
-        if (model == MCGB_MODEL_KAWAMURA) {
+        if (model == MCGB_MODEL_KAWAMURA || model == MCGB_MODEL_KAWAMURA_GAUSS) {
             const float *b = static_cast<const float *>(state) + 5 * rep.state_offset;
             const float *a = cm_site(b, i, j, L, 5);
             const float *nbs[2] = {cm_site(b, id, j, L, 5), cm_site(b, i, jr, L, 5)};
@@ -577,11 +615,14 @@ int continuum_launch(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_
 int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx)
 {
     if (int st = validate_window(w)) return st;
-    MCGB_REQUIRE(model != MCGB_MODEL_KAWAMURA || w.aux != nullptr, "Kawamura window: null (cos, sin) cache");
+    MCGB_REQUIRE((model != MCGB_MODEL_KAWAMURA && model != MCGB_MODEL_KAWAMURA_GAUSS) || w.aux != nullptr,
+                 "Kawamura window: null (cos, sin) cache");
     BatchArgs a = make_args(w);
     if (fx != nullptr) a.fx = *fx;
     switch (model) {
-    case MCGB_MODEL_KAWAMURA: return continuum_launch<KawamuraPolicy>(a, w, s, "kawamura window");
+    case MCGB_MODEL_KAWAMURA: return continuum_launch<KawamuraPolicy<false>>(a, w, s, "kawamura window");
+    case MCGB_MODEL_KAWAMURA_GAUSS:
+        return continuum_launch<KawamuraPolicy<true>>(a, w, s, "kawamura gaussian window");
     case MCGB_MODEL_HE3: return continuum_launch<He3Policy<false>>(a, w, s, "he3 window");
     default: return continuum_launch<He3Policy<true>>(a, w, s, "he3 gaussian window");
     }
@@ -589,7 +630,8 @@ int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s, cons
 
 int64_t continuum_smem(int model, int L, int C)
 {
-    if (model == MCGB_MODEL_KAWAMURA) return (int64_t)single_smem<KawamuraPolicy>(L, C);
+    if (model == MCGB_MODEL_KAWAMURA || model == MCGB_MODEL_KAWAMURA_GAUSS)
+        return (int64_t)single_smem<KawamuraPolicy<false>>(L, C);
     return (int64_t)single_smem<He3Policy<false>>(L, C);
 }
 
@@ -603,7 +645,8 @@ int continuum_clusters(int C, int threads, size_t smem, int *out)
 int continuum_max_clusters(int model, int C, int threads, size_t smem, int *out)
 {
     switch (model) {
-    case MCGB_MODEL_KAWAMURA: return continuum_clusters<KawamuraPolicy>(C, threads, smem, out);
+    case MCGB_MODEL_KAWAMURA: return continuum_clusters<KawamuraPolicy<false>>(C, threads, smem, out);
+    case MCGB_MODEL_KAWAMURA_GAUSS: return continuum_clusters<KawamuraPolicy<true>>(C, threads, smem, out);
     case MCGB_MODEL_HE3: return continuum_clusters<He3Policy<false>>(C, threads, smem, out);
     default: return continuum_clusters<He3Policy<true>>(C, threads, smem, out);
     }

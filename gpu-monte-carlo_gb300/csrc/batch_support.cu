@@ -62,14 +62,15 @@ __global__ void tune_sigma_kernel(float *sigma_t, const long long *accepted, lon
 using namespace mcgb;
 
 static bool is_lattice(int model) { return model == MCGB_MODEL_ISING || model == MCGB_MODEL_XY; }
-static bool known_model(int model) { return model >= MCGB_MODEL_ISING && model <= MCGB_MODEL_HE3_GAUSS; }
+static bool known_model(int model) { return model >= MCGB_MODEL_ISING && model <= MCGB_MODEL_KAWAMURA_GAUSS; }
 
 extern "C" int mcgb_batch_channels(int model)
 {
     switch (model) {
     case MCGB_MODEL_ISING: return 2;
     case MCGB_MODEL_XY: return 5;
-    case MCGB_MODEL_KAWAMURA: return 7;
+    case MCGB_MODEL_KAWAMURA:
+    case MCGB_MODEL_KAWAMURA_GAUSS: return 7;
     case MCGB_MODEL_HE3:
     case MCGB_MODEL_HE3_GAUSS: return 10;
     default: set_error("unknown model %d", model); return MCGB_EINVAL;
@@ -101,6 +102,7 @@ extern "C" int mcgb_batch_window_run(int model, const mcgb_batch_window *w, void
     MCGB_REQUIRE(w != nullptr, "batch window: null argument block");
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
+    if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream))
                              : continuum_window(model, *w, as_stream(stream));
 }
@@ -118,7 +120,7 @@ extern "C" int mcgb_batch_refresh_aux(int model, const mcgb_batch_window *w, voi
 {
     MCGB_REQUIRE(w != nullptr, "refresh_aux: null argument block");
     if (model == MCGB_MODEL_XY) return refresh_aux(*w, 1, as_stream(stream));
-    if (model == MCGB_MODEL_KAWAMURA) return refresh_aux(*w, 5, as_stream(stream));
+    if (model == MCGB_MODEL_KAWAMURA || model == MCGB_MODEL_KAWAMURA_GAUSS) return refresh_aux(*w, 5, as_stream(stream));
     return MCGB_OK;
 }
 
@@ -162,6 +164,7 @@ extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w,
     if (int st = check_exchange(*w, *pt)) return st;
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
+    if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
     FusedExchange fx;
     fx.ex = make_exchange_args(*w, *pt);
     fx.ladder_done = sync;

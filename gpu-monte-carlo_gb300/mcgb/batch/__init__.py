@@ -31,7 +31,7 @@ from ..rng import create_xoroshiro128p_states
 REPLICA_DTYPE = np.dtype([("L", "<i4"), ("ladder", "<i4"), ("ladder_start", "<i4"),
                           ("n_temps", "<i4"), ("state_offset", "<i8")])
 
-MODEL_ISING, MODEL_XY, MODEL_KAWAMURA, MODEL_HE3, MODEL_HE3_GAUSS = range(5)
+MODEL_ISING, MODEL_XY, MODEL_KAWAMURA, MODEL_HE3, MODEL_HE3_GAUSS, MODEL_KAWAMURA_GAUSS = range(6)
 
 CHANNELS = {
     MODEL_ISING: ("energy", "magnetization"),
@@ -41,6 +41,9 @@ CHANNELS = {
                 "current_x", "curvature_x", "current_y", "curvature_y", "spin_alignment"),
 }
 CHANNELS[MODEL_HE3_GAUSS] = CHANNELS[MODEL_HE3]
+CHANNELS[MODEL_KAWAMURA_GAUSS] = CHANNELS[MODEL_KAWAMURA]
+# Models whose proposals have per-temperature widths sigma_t.
+GAUSSIAN_WIDTHS = (MODEL_XY, MODEL_KAWAMURA_GAUSS)
 
 
 class BatchWindow(ctypes.Structure):
@@ -74,7 +77,7 @@ class BatchPT(ctypes.Structure):
     ]
 
 
-def _model_info(model, gaussian):
+def _model_info(model, gaussian, proposal="uniform"):
     from ..models.he3.model import He3Model
     from ..models.ising.model import IsingModel
     from ..models.kawamura.model import KawamuraModel
@@ -85,7 +88,7 @@ def _model_info(model, gaussian):
     if isinstance(model, XYModel):
         return MODEL_XY, np.dtype(np.float32), ()
     if isinstance(model, KawamuraModel):
-        return MODEL_KAWAMURA, np.dtype(np.float32), (5,)
+        return (MODEL_KAWAMURA_GAUSS if proposal == "gaussian" else MODEL_KAWAMURA), np.dtype(np.float32), (5,)
     if isinstance(model, He3Model):
         return (MODEL_HE3_GAUSS if gaussian else MODEL_HE3), np.dtype(np.complex64), (3, 2)
     raise TypeError(f"unsupported model {type(model).__name__}")
@@ -141,7 +144,7 @@ class LadderBatch:
                  proposal="uniform", sigma0=1.0, gaussian=False, rho=-0.9, proposal_mass=0.0,
                  cluster_size=None, threads=None, initial_states=None):
         self.model = model
-        self.model_id, self.dtype, self.site_shape = _model_info(model, gaussian)
+        self.model_id, self.dtype, self.site_shape = _model_info(model, gaussian, proposal)
         self.channels = CHANNELS[self.model_id]
         self.pt = exchange_interval is not None
         if self.pt and (isinstance(exchange_interval, bool) or int(exchange_interval) != exchange_interval
@@ -165,8 +168,11 @@ class LadderBatch:
         self.exchange_seeds = ([s + 1 for s in self.seeds] if exchange_seeds is None
                                else [int(s) for s in exchange_seeds])
         self.proposal = proposal
-        if self.model_id == MODEL_XY and proposal not in ("uniform", "gaussian"):
+        if proposal not in ("uniform", "gaussian"):
             raise ValueError("proposal must be 'uniform' or 'gaussian'")
+        if proposal == "gaussian" and self.model_id not in GAUSSIAN_WIDTHS:
+            raise ValueError("Gaussian widths apply to the XY and Kawamura models "
+                             "(He3 selects its sampler with gaussian=True)")
 
         # ---------------------------------------------------------- replica table
         rows, starts, sizes, offset = [], [], [], 0
@@ -227,7 +233,7 @@ class LadderBatch:
         self.sigma_t = to_device(np.full(self.R, sigma0, np.float32))
         self.staging = device_zeros((len(self.channels), self.R), np.float64)
         self.aux = (DeviceArray((self.n_sites, 2), np.float32)
-                    if self.model_id in (MODEL_XY, MODEL_KAWAMURA) else None)
+                    if self.model_id in (MODEL_XY, MODEL_KAWAMURA, MODEL_KAWAMURA_GAUSS) else None)
         self.sweeps = 0
         self.exchange_rounds = 0
 
@@ -337,7 +343,8 @@ class LadderBatch:
             if smem > 232448:
                 continue
             npl_max = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in np.unique(Ls))
-            t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512}.get(self.model_id, 1024)
+            t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512,
+                     MODEL_KAWAMURA_GAUSS: 512}.get(self.model_id, 1024)
             for T in (128, 256, 512, 1024):
                 if T > t_max or (T > 32 * ((npl_max + 31) // 32) and T > 128):
                     continue
@@ -414,11 +421,14 @@ class LadderBatch:
         w.n_sweeps = int(n_sweeps)
         w.J = float(getattr(self.model, "J", 1.0))
         w.delta = float(getattr(self.model, "delta", 0.0))
-        w.sigma_t = self.sigma_t.ptr if (self.model_id == MODEL_XY and self.proposal == "gaussian") else None
+        w.sigma_t = self.sigma_t.ptr if self._gaussian_widths() else None
         for q in range(5):
             w.coefficients[q] = float(self.coefficients[q])
         w.K, w.g_d, w.rho, w.mass = self.K, self.g_d, self.rho, self.mass
         return w
+
+    def _gaussian_widths(self):
+        return self.model_id in GAUSSIAN_WIDTHS and self.proposal == "gaussian"
 
     def _pt(self):
         p = BatchPT()
@@ -608,7 +618,7 @@ class LadderBatch:
         if sample_interval < 1 or sample_interval > measurement_sweeps:
             raise ValueError("Invalid sampling interval")
         if tune_sigma is None:
-            tune_sigma = self.model_id == MODEL_XY and self.proposal == "gaussian"
+            tune_sigma = self._gaussian_widths()
         start = self.sweeps
         self.samples = None
         self.run(thermalization_sweeps, tune=tune_sigma, graph=graph)

@@ -187,6 +187,8 @@ enum {
     MCGB_MODEL_KAWAMURA = 2,
     MCGB_MODEL_HE3 = 3,       /* Cartesian proposals */
     MCGB_MODEL_HE3_GAUSS = 4, /* conditional Gaussian MH proposals */
+    MCGB_MODEL_KAWAMURA_GAUSS = 5, /* Gaussian MH proposals (theta and d), widths sigma_t;
+                                      no reference counterpart */
 };
 
 typedef struct mcgb_replica {

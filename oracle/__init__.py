@@ -71,6 +71,8 @@ def _declare(L):
         "orc_kawamura_local_energy": (_F, [_P, _I, _I, _I, _I, _F, _F, _F, _F, _F, _F]),
         "orc_kawamura_update_color": (None, [_P, _P, _P, _I, _I, _I, _F, _F]),
         "orc_kawamura_sweeps": (None, [_P, _P, _P, _I, _I, _F, _F, _I, _I]),
+        "orc_kawamura_update_color_gauss": (None, [_P, _P, _P, _P, _I, _I, _I, _F]),
+        "orc_kawamura_sweeps_gauss": (None, [_P, _P, _P, _P, _I, _I, _F, _I, _I]),
         "orc_kawamura_energy": (None, [_P, _I, _I, _F, _P]),
         "orc_kawamura_measure": (None, [_P, _I, _I, _F, _P, _P, _P]),
         "orc_he3_potential": (_F, [_P, _P, _F]),
@@ -238,6 +240,20 @@ def kawamura_sweeps(state, rng, betas, J, delta, n_sweeps, n_threads=1):
     R, L = state.shape[0], state.shape[1]
     lib().orc_kawamura_sweeps(_ptr(_check(state, np.float32, "state")), _ptr(_check(rng, np.uint64, "rng")),
                               _ptr(_check(betas, np.float32, "betas")), R, L, J, delta, n_sweeps, n_threads)
+
+
+def kawamura_update_color_gauss(state, rng, betas, sigmas, color, J):
+    R, L = state.shape[0], state.shape[1]
+    lib().orc_kawamura_update_color_gauss(_ptr(_check(state, np.float32, "state")), _ptr(_check(rng, np.uint64, "rng")),
+                                          _ptr(_check(betas, np.float32, "betas")),
+                                          _ptr(_check(sigmas, np.float32, "sigmas")), R, L, color, J)
+
+
+def kawamura_sweeps_gauss(state, rng, betas, sigmas, J, n_sweeps, n_threads=1):
+    R, L = state.shape[0], state.shape[1]
+    lib().orc_kawamura_sweeps_gauss(_ptr(_check(state, np.float32, "state")), _ptr(_check(rng, np.uint64, "rng")),
+                                    _ptr(_check(betas, np.float32, "betas")),
+                                    _ptr(_check(sigmas, np.float32, "sigmas")), R, L, J, n_sweeps, n_threads)
 
 
 def kawamura_energy(state, J):

@@ -389,6 +389,96 @@ static void kawamura_color_replica(float *state, uint64_t *rng, float beta, int 
         }
 }
 
+/* Gaussian proposals (this project's extension; the three sub-moves and   */
+/* their acceptance rule are the reference's): theta' = theta + sigma*z0,   */
+/* wrapped; tau flipped; d' = (d + sigma*g)/|d + sigma*g| with g three      */
+/* standard normals (symmetric: its density depends only on the angle       */
+/* between d and d').  Five draws per visit: two Box-Muller pairs (z0, gx)  */
+/* and (gy, gz), each from bits 63..41 and 40..18 of one draw, then the     */
+/* three acceptance uniforms.                                               */
+static void box_muller_pair(uint64_t x, float *z1, float *z2)
+{
+    float u1 = (float)(x >> 41) * 0x1p-23f;
+    float u2 = (float)((x >> 18) & 0x7fffffu) * 0x1p-23f;
+    if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
+    float rad = sqrtf(-2.0f * logf(u1));
+    float ang = TWO_PI_F * u2;
+    *z1 = rad * cosf(ang);
+    *z2 = rad * sinf(ang);
+}
+
+static void kawamura_gauss_color_replica(float *state, uint64_t *rng, float beta, int r, int L,
+                                         int color, float J, float sigma)
+{
+    for (int i = color / 2; i < L; i += 2)
+        for (int j = color % 2; j < L; j += 2) {
+            float *site = state + (((int64_t)r * L + i) * L + j) * 5;
+            int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
+            uint64_t *st = rng + 2 * idx;
+            float theta = site[0], tau = site[1], dx = site[2], dy = site[3], dz = site[4];
+            float z0, gx, gy, gz;
+            box_muller_pair(orc_rng_next(st), &z0, &gx);
+            box_muller_pair(orc_rng_next(st), &gy, &gz);
+            float energy = orc_kawamura_local_energy(state, L, r, i, j, theta, tau, dx, dy, dz, J);
+
+            float pt = theta + sigma * z0;
+            pt -= TWO_PI_F * floorf((pt + PI_F) / TWO_PI_F);
+            if (pt >= PI_F) pt -= TWO_PI_F;
+            if (pt < -PI_F) pt += TWO_PI_F;
+            float pe = orc_kawamura_local_energy(state, L, r, i, j, pt, tau, dx, dy, dz, J);
+            float dE = pe - energy;
+            float u = orc_rng_uniform_f32(st);
+            if (dE <= 0.0f || u < expf(-beta * dE)) {
+                theta = pt;
+                energy = pe;
+            }
+
+            float ptau = -tau;
+            pe = orc_kawamura_local_energy(state, L, r, i, j, theta, ptau, dx, dy, dz, J);
+            dE = pe - energy;
+            u = orc_rng_uniform_f32(st);
+            if (dE <= 0.0f || u < expf(-beta * dE)) {
+                tau = ptau;
+                energy = pe;
+            }
+
+            float x = dx + sigma * gx, y = dy + sigma * gy, z = dz + sigma * gz;
+            float inv = 1.0f / sqrtf((x * x + y * y) + z * z);
+            x *= inv;
+            y *= inv;
+            z *= inv;
+            pe = orc_kawamura_local_energy(state, L, r, i, j, theta, tau, x, y, z, J);
+            dE = pe - energy;
+            u = orc_rng_uniform_f32(st);
+            if (dE <= 0.0f || u < expf(-beta * dE)) {
+                dx = x;
+                dy = y;
+                dz = z;
+            }
+            site[0] = theta;
+            site[1] = tau;
+            site[2] = dx;
+            site[3] = dy;
+            site[4] = dz;
+        }
+}
+
+void orc_kawamura_update_color_gauss(float *state, uint64_t *rng, const float *betas, const float *sigmas,
+                                     int R, int L, int color, float J)
+{
+    for (int r = 0; r < R; ++r) kawamura_gauss_color_replica(state, rng, betas[r], r, L, color, J, sigmas[r]);
+}
+
+void orc_kawamura_sweeps_gauss(float *state, uint64_t *rng, const float *betas, const float *sigmas, int R,
+                               int L, float J, int n_sweeps, int n_threads)
+{
+    (void)n_threads;
+    OMP_FOR_R
+    for (int r = 0; r < R; ++r)
+        for (int s = 0; s < n_sweeps; ++s)
+            for (int c = 0; c < 4; ++c) kawamura_gauss_color_replica(state, rng, betas[r], r, L, c, J, sigmas[r]);
+}
+
 void orc_kawamura_update_color(float *state, uint64_t *rng, const float *betas, int R, int L,
                                int color, float J, float delta)
 {

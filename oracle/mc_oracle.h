@@ -68,6 +68,10 @@ void orc_kawamura_update_color(float *state, uint64_t *rng, const float *betas,
                                int R, int L, int color, float J, float delta);
 void orc_kawamura_sweeps(float *state, uint64_t *rng, const float *betas,
                          int R, int L, float J, float delta, int n_sweeps, int n_threads);
+void orc_kawamura_update_color_gauss(float *state, uint64_t *rng, const float *betas,
+                                     const float *sigmas, int R, int L, int color, float J);
+void orc_kawamura_sweeps_gauss(float *state, uint64_t *rng, const float *betas, const float *sigmas,
+                               int R, int L, float J, int n_sweeps, int n_threads);
 void orc_kawamura_energy(const float *state, int R, int L, float J, double *out);
 void orc_kawamura_measure(const float *state, int R, int L, float J,
                           const int32_t *temperature_indices, const double *cached,

@@ -8,7 +8,8 @@
   below, written independently of the C oracle: raw 64-bit outputs and the
   float64/float32 uniforms (top 53 bits x 2^-53, the float32 one rounded
   from the float64), for several seeds and stream indices.
-* ``sweeps.npz`` -- small seeded runs of every update rule through the C
+* ``sweeps.npz`` -- small seeded runs of every update rule (and of the XY and
+  Kawamura Gaussian proposals) through the C
   oracle (the reference kernels restated): inputs, final states and RNG
   streams after a few four-colour sweeps, and the measurement channels of
   the final states.
@@ -159,6 +160,11 @@ def sweep_fixture():
     oracle.kawamura_sweeps(state, rng, betas, np.float32(1), np.float32(1.5), 3)
     out.update({"kaw_seed": seed, "kaw_betas": betas, "kaw_in": st, "kaw_sweeps": 3, "kaw_out": state,
                 "kaw_rng_out": rng, "kaw_measure": oracle.kawamura_measure(state, np.float32(1))})
+    # ... and with Gaussian proposals (this project's extension).
+    sig = np.array([0.6, 0.8], np.float32)
+    state, rng = st.copy(), oracle.rng_states(2 * L * L, seed)
+    oracle.kawamura_sweeps_gauss(state, rng, betas, sig, np.float32(1), 3)
+    out.update({"kawg_sigmas": sig, "kawg_out": state, "kawg_rng_out": rng})
 
     # He3 (class defaults): Cartesian and conditional-Gaussian proposals, 2 sweeps.
     L, T, seed = 8, np.array([0.35, 0.45]), 50

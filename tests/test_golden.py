@@ -81,6 +81,15 @@ def test_kawamura_fixture(sweeps):
     np.testing.assert_array_equal(oracle.kawamura_measure(state, np.float32(1)), s["kaw_measure"])
 
 
+def test_kawamura_gaussian_fixture(sweeps):
+    s = sweeps
+    state = s["kaw_in"].copy()
+    rng = oracle.rng_states(state.shape[0] * state.shape[1] ** 2, int(s["kaw_seed"]))
+    oracle.kawamura_sweeps_gauss(state, rng, s["kaw_betas"], s["kawg_sigmas"], np.float32(1), int(s["kaw_sweeps"]))
+    np.testing.assert_array_equal(state, s["kawg_out"])
+    np.testing.assert_array_equal(rng, s["kawg_rng_out"])
+
+
 @pytest.mark.parametrize("name", ["he3", "he3g"])
 def test_he3_fixtures(sweeps, name):
     s = sweeps

@@ -233,6 +233,30 @@ def test_kawamura_batch_sweep_matches_oracle_and_tracks_energy():
     assert set(np.unique(st[..., 1])) <= {-1.0, 1.0}
 
 
+def test_kawamura_gaussian_batch_sweep_matches_oracle():
+    """Gaussian proposals (theta and d) against the oracle's restatement:
+    streams bit-exact (five draws per visit), sites within float32 rounding."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.kawamura.model import KawamuraModel
+    L, temps = 32, np.linspace(0.65, 0.8, 4)
+    init = npref.random_kawamura(np.random.default_rng(19), 4, L)
+    sig = np.array([0.5, 0.6, 0.7, 0.8], np.float32)
+    b = LadderBatch(KawamuraModel(), [(L, temps)], seeds=[18], exchange_interval=None, proposal="gaussian",
+                    cluster_size=2, threads=256, initial_states=[init])
+    b.sigma_t.copy_to_device(sig)
+    e0 = b.energies.copy_to_host()
+    b.run(2)
+    ref, rr = init.copy(), oracle.rng_states(4 * L * L, 18)
+    oracle.kawamura_sweeps_gauss(ref, rr, (1 / temps).astype(np.float32), sig, np.float32(1), 2)
+    np.testing.assert_array_equal(b.ladder_rng(0), rr)
+    got = b.ladder_state(0)
+    assert_close_sites(got, ref, -1)
+    d_run = b.energies.copy_to_host() - e0
+    d_exact = npref.kawamura(got, 1.0)["energy"] - e0
+    assert np.all(np.abs(d_run - d_exact) <= 1e-5 * np.abs(d_exact))
+    np.testing.assert_allclose(np.linalg.norm(got[..., 2:], axis=-1), 1, atol=3e-6)
+
+
 def test_kawamura_batch_pt_samples_match_numpy():
     from mcgb.batch import LadderBatch
     from mcgb.models.kawamura.model import KawamuraModel

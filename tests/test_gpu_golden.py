@@ -113,6 +113,21 @@ def test_kawamura_golden_sweeps(fx):
                    fx["kaw_measure"])
 
 
+def test_kawamura_gaussian_golden_sweeps(fx):
+    from mcgb.batch import LadderBatch
+    from mcgb.models.kawamura.model import KawamuraModel
+    init = fx["kaw_in"]
+    T = 1.0 / fx["kaw_betas"].astype(np.float64)
+    b = LadderBatch(KawamuraModel(), [(init.shape[1], T)], seeds=[int(fx["kaw_seed"])], exchange_interval=None,
+                    proposal="gaussian", initial_states=[init])
+    b.betas.copy_to_device(fx["kaw_betas"])
+    b.sigma_t.copy_to_device(fx["kawg_sigmas"])
+    b.run(int(fx["kaw_sweeps"]))
+    rng = b.ladder_rng(0)
+    np.testing.assert_array_equal(rng, fx["kawg_rng_out"])
+    _states_close(b.ladder_state(0), fx["kawg_out"], (-1,))
+
+
 @pytest.mark.parametrize("name", ["he3", "he3g"])
 def test_he3_golden_sweeps(fx, name):
     from mcgb import device

@@ -129,3 +129,39 @@ def test_he3_conditional_gaussian_batch_samples_the_cartesian_distribution():
     g = stats.he3_observables(run["samples"], L, T, block_size=block)
     assert_agree(a, g)
     assert np.all(np.isfinite(a["energy"][1])) and np.all(a["energy"][1] > 0)
+
+
+def test_kawamura_gaussian_batch_matches_reference_on_independent_replicas():
+    """Gaussian theta/d proposals (batch) against the reference's uniform,
+    flip and sphere proposals (drop-in Runtime): energy and the three order
+    parameters of the Kawamura analysis, jackknifed over 96 independent
+    replicas per temperature."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.kawamura.model import KawamuraModel
+    L, n = 8, 96
+    temps = np.repeat([0.6, 0.9], n)
+    groups = [slice(0, n), slice(n, 2 * n)]
+    therm, meas, interval = 2000, 20000, 10
+
+    ref = dropin_simulation(KawamuraModel(), L, temps, 42 + L, therm, meas, interval, pt=False)
+    b = LadderBatch(KawamuraModel(), [(L, temps)], seeds=[1042 + L], exchange_interval=None, proposal="gaussian",
+                    sigma0=0.5)
+    run = b.simulate(thermalization_sweeps=therm, measurement_sweeps=meas, sample_interval=interval)[0]
+
+    def observables(samples):
+        out = {k: ([], []) for k in ("energy", "chirality", "phase", "spin")}
+        for idx in groups:
+            per = {"e": samples["energy"][:, idx].mean(0) / L ** 2,
+                   "tau2": (samples["chirality"][:, idx] ** 2).mean(0) / L ** 4,
+                   "phase2": (samples["px"][:, idx] ** 2 + samples["py"][:, idx] ** 2).mean(0) / L ** 4,
+                   "spin2": samples["spin2"][:, idx].mean(0) / L ** 4}
+            v, e = stats.jackknife(per, lambda m: np.stack((m["e"], np.sqrt(m["tau2"]), np.sqrt(m["phase2"]),
+                                                            np.sqrt(m["spin2"]))), 1)
+            for k, name in enumerate(out):
+                out[name][0].append(v[k])
+                out[name][1].append(e[k])
+        return {k: (np.array(v), np.array(e)) for k, (v, e) in out.items()}
+
+    a, g = observables(ref["samples"]), observables(run["samples"])
+    assert_agree(a, g)
+    assert np.all(a["energy"][1] < 2e-3) and abs(a["energy"][0][0] - a["energy"][0][1]) > 0.1
