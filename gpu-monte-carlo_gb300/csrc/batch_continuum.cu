@@ -49,7 +49,9 @@ struct KawamuraPolicy {
     static constexpr int kChannels = 7;   // energy, chirality, px, py, spin2, twist_cos_x, twist_sin_x
     static constexpr int kSums = 12;      // ... with the six spin-tensor sums in place of spin2
     static constexpr int kMaxThreads = 512;
+    static constexpr int kPairThreads = 256;  // two plaquettes a thread spill at 128 registers
     static constexpr bool kSplitMiddle = false;
+    static constexpr bool kPipeline = true;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 
@@ -267,26 +269,27 @@ __device__ __forceinline__ float he3_potential_f(const c32 *psi, const float *be
     return -2.0f * n + beta[0] * i1 + beta[1] * i2 + beta[2] * i3 + beta[3] * i4 + beta[4] * i5 + g_d * dip;
 }
 
+// The six neighbour cells a visit reads: the four nearest and the far
+// corners (i-1, j+1), (i+1, j-1) of the site's three forward gradient cells.
+struct He3Nbrs {
+    const He3Cell *R, *U, *Lf, *D, *LU, *DR;  // (i+1,j) (i,j+1) (i-1,j) (i,j-1) (i-1,j+1) (i+1,j-1)
+};
+
 // Exact change of the three gradient cells containing the site when its
 // components change from cur to nxt (models/he3/update.py:95-175).
-template <int C_>
-__device__ __forceinline__ float he3_grad_diff(const Nbrs<He3Cell> &nb, const He3Cell &cur, const c32 *nxt)
+__device__ __forceinline__ float he3_grad_diff(const He3Nbrs &n, const He3Cell &cur, const c32 *nxt)
 {
-    const He3Cell &R = MCGB_NBR(nb, kDown(C_));       // (i+1, j)
-    const He3Cell &U = MCGB_NBR(nb, kRight(C_));      // (i, j+1)
-    const He3Cell &Lf = MCGB_NBR(nb, kUp(C_));        // (i-1, j)
-    const He3Cell &D = MCGB_NBR(nb, kLeft(C_));       // (i, j-1)
-    const He3Cell &LU = MCGB_NBR(nb, kUpRight(C_));   // (i-1, j+1)
-    const He3Cell &DR = MCGB_NBR(nb, kDownLeft(C_));  // (i+1, j-1)
     float dg = 0.0f;
 #pragma unroll
     for (int mu = 0; mu < 3; ++mu) {
         const int kx = 2 * mu, ky = 2 * mu + 1;
         const c32 x = cur.z[kx], y = cur.z[ky];
         const c32 ex = nxt[kx] - x, ey = nxt[ky] - y;
-        const c32 a = R.z[kx] - x, b = R.z[ky] - y, c = U.z[kx] - x, d = U.z[ky] - y;
-        const c32 al = x - Lf.z[kx], bl = y - Lf.z[ky], cl = LU.z[kx] - Lf.z[kx], dl = LU.z[ky] - Lf.z[ky];
-        const c32 ad = DR.z[kx] - D.z[kx], bd = DR.z[ky] - D.z[ky], cd = x - D.z[kx], dd = y - D.z[ky];
+        const c32 a = n.R->z[kx] - x, b = n.R->z[ky] - y, c = n.U->z[kx] - x, d = n.U->z[ky] - y;
+        const c32 al = x - n.Lf->z[kx], bl = y - n.Lf->z[ky], cl = n.LU->z[kx] - n.Lf->z[kx],
+                  dl = n.LU->z[ky] - n.Lf->z[ky];
+        const c32 ad = n.DR->z[kx] - n.D->z[kx], bd = n.DR->z[ky] - n.D->z[ky], cd = x - n.D->z[kx],
+                  dd = y - n.D->z[ky];
         const c32 fx = (-(3.0f * a + b + c + d) + (3.0f * al + dl)) + (cd + bd);
         const c32 fy = (-(a + b + c + 3.0f * d) + (bl + cl)) + (3.0f * dd + ad);
         const float linear = 2.0f * (conj(ex) * fx + conj(ey) * fy).re;
@@ -296,6 +299,126 @@ __device__ __forceinline__ float he3_grad_diff(const Nbrs<He3Cell> &nb, const He
     return dg;
 }
 
+struct He3Ctx {
+    float beta, K, delta, g_d, rho, mass;
+    float coeff[5];
+    long long *nonfinite;  // counters row 2 entry of this replica
+};
+
+struct He3Visit {
+    ulonglong2 st;
+    float dE;
+    int accepted;
+};
+
+// gaussian_fast.py:42-50 with fast intrinsics: a pair of standard normals.
+__device__ __forceinline__ c32 he3_normal_pair(ulonglong2 &st)
+{
+    float u = mcgb_fast_unit(xoro_next(st));
+    if (u <= 0.0f) u = 1.1102230246251565e-16f;
+    const float ang = kTwoPi * mcgb_fast_unit(xoro_next(st));
+    const float t = -2.0f * __logf(u);
+    const float rad = t * rsqrtf(t);
+    float sn, cs;
+    __sincosf(ang - kPi, &sn, &cs);  // cos(ang) = -cs, sin(ang) = -sn
+    return cmk(-rad * cs, -rad * sn);
+}
+
+// One visit of one site: every draw, in the reference's order, and the
+// decision.  Out of line and independent of the colour (the neighbours come
+// as pointers), so the window kernel holds one copy of this long body rather
+// than one per colour and plaquette slot: the unrolled copies overflowed the
+// instruction cache.
+//   Cartesian (models/he3/update.py:178-227): twelve offsets, then the
+//     acceptance uniform; potential change plus the exact gradient change.
+//   Conditional Gaussian (gaussian_fast.py:26-119): six Box-Muller pairs, the
+//     acceptance uniform; neighbour field, autoregressive proposal, reverse /
+//     forward log density ratio, full Hamiltonian change.  Nonfinite log
+//     ratios are counted per replica and rejected.
+template <bool kGauss>
+__device__ __noinline__ He3Visit he3_visit(const He3Ctx x, const He3Nbrs n, He3Cell *site, ulonglong2 st)
+{
+    He3Visit out;
+    out.accepted = 0;
+    out.dE = 0.0f;
+    const He3Cell me = *site;
+    if constexpr (!kGauss) {
+        c32 w[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float re = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
+            const float im = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
+            w[k] = cmk(me.z[k].re + re, me.z[k].im + im);
+        }
+        const float v = mcgb_fast_unit(xoro_next(st));
+        const float dv = he3_potential_f(w, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d);
+        const float diff = dv + x.K * he3_grad_diff(n, me, w);
+        if (diff <= 0.0f || v < __expf(-x.beta * diff)) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) site->z[k] = w[k];
+            out.dE = diff;
+            out.accepted = 1;
+        }
+        out.st = st;
+        return out;
+    } else {
+    c32 zz[6];
+#pragma unroll
+    for (int mu = 0; mu < 3; ++mu) {
+        zz[2 * mu] = he3_normal_pair(st);      // zp
+        zz[2 * mu + 1] = he3_normal_pair(st);  // zm
+    }
+    const float v = mcgb_fast_unit(xoro_next(st));
+    out.st = st;
+    const float root = 0.7071067811865475f;
+    const float plus = 10.0f * x.K + x.mass, minus = 6.0f * x.K + x.mass;
+    const float vf = 1.0f - x.rho * x.rho;
+    const float sp = sqrtf(vf / (2.0f * x.beta * plus));
+    const float sm = sqrtf(vf / (2.0f * x.beta * minus));
+    const float qp = vf / (8.0f * root * root * sp * sp);
+    const float qm = vf / (8.0f * root * root * sm * sm);
+    c32 nxt[6];
+    float lpr = 0.0f;
+#pragma unroll
+    for (int mu = 0; mu < 3; ++mu) {
+        const int kx = 2 * mu, ky = 2 * mu + 1;
+        const c32 f0 = -3.0f * (n.R->z[kx] + n.Lf->z[kx]) - n.U->z[kx] - n.U->z[ky] - n.R->z[ky] - n.Lf->z[ky] -
+                       n.D->z[kx] - n.D->z[ky] + n.LU->z[ky] + n.DR->z[ky];
+        const c32 f1 = -n.R->z[kx] - n.R->z[ky] - n.U->z[kx] - n.Lf->z[kx] - n.Lf->z[ky] - n.D->z[kx] -
+                       3.0f * (n.U->z[ky] + n.D->z[ky]) + n.LU->z[kx] + n.DR->z[kx];
+        const c32 xo = me.z[kx], yo = me.z[ky];
+        const c32 hp = root * (f0 + f1), hm = root * (f0 - f1);
+        c32 mp = (-x.K) * hp, mm = (-x.K) * hm;
+        mp = cmk(mp.re / plus, mp.im / plus);
+        mm = cmk(mm.re / minus, mm.im / minus);
+        const c32 mx = root * (mp + mm), my = root * (mp - mm);
+        const c32 zp = sp * zz[kx], zm = sm * zz[ky];
+        const c32 nx = (mx + x.rho * (xo - mx)) + root * (zp + zm);
+        const c32 ny = (my + x.rho * (yo - my)) + root * (zp - zm);
+        nxt[kx] = nx;
+        nxt[ky] = ny;
+        const c32 op = (xo - mx) + (yo - my), om = (xo - mx) - (yo - my);
+        const c32 np = (nx - mx) + (ny - my), nm = (nx - mx) - (ny - my);
+        lpr += qp * (norm2(np) - norm2(op));
+        lpr += qm * (norm2(nm) - norm2(om));
+    }
+    const float dh = he3_potential_f(nxt, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d) +
+                     x.K * he3_grad_diff(n, me, nxt);
+    const float log_ratio = -x.beta * dh + lpr;
+    if (!isfinite(log_ratio)) {
+        if (x.nonfinite) atomicAdd(reinterpret_cast<unsigned long long *>(x.nonfinite), 1ull);
+        return out;
+    }
+    if (log_ratio >= 0.0f || v < __expf(log_ratio)) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) site->z[k] = nxt[k];
+        out.dE = dh;
+        out.accepted = 1;
+    }
+    return out;
+    }
+}
+
 template <bool kGauss>
 struct He3Policy {
     using Args = BatchArgs;
@@ -303,21 +426,15 @@ struct He3Policy {
     static constexpr int kOwnFloats = 0;
     static constexpr int kChannels = 10;
     static constexpr int kSums = 10;  // the last sum is the spin-z density until finish_sample
-    static constexpr int kMaxThreads = 256;
+    static constexpr int kMaxThreads = 256;  // the visit needs ~250 registers
+    static constexpr int kPairThreads = 256;
     static constexpr bool kSplitMiddle = true;
+    static constexpr bool kPipeline = false;  // update<c>: one out-of-line visit
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 
-    struct Ctx {
-        float beta, K, delta, g_d, rho, mass;
-        float coeff[5];
-        long long *nonfinite;  // counters row 2 entry of this replica
-    };
-    struct Prop {
-        c32 w[6];   // Cartesian: proposed components; Gaussian: the six standard normal pairs
-        float dv;   // Cartesian: potential change
-        float v;    // acceptance uniform
-    };
+    using Ctx = He3Ctx;
+    struct Prop {};
 
     static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
     {
@@ -350,108 +467,16 @@ struct He3Policy {
         for (int q = 0; q < 3; ++q)
             p[q] = make_float4(cell.z[2 * q].re, cell.z[2 * q].im, cell.z[2 * q + 1].re, cell.z[2 * q + 1].im);
     }
-    // gaussian_fast.py:42-50 with fast intrinsics: a pair of standard normals.
-    static __device__ __forceinline__ c32 normal_pair(ulonglong2 &st)
-    {
-        float u = mcgb_fast_unit(xoro_next(st));
-        if (u <= 0.0f) u = 1.1102230246251565e-16f;
-        const float ang = kTwoPi * mcgb_fast_unit(xoro_next(st));
-        const float t = -2.0f * __logf(u);
-        const float rad = t * rsqrtf(t);
-        float sn, cs;
-        __sincosf(ang - kPi, &sn, &cs);  // cos(ang) = -cs, sin(ang) = -sn
-        return cmk(-rad * cs, -rad * sn);
-    }
     template <int C_>
-    static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &me, const float *, ulonglong2 &st)
+    static __device__ __forceinline__ bool update(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *,
+                                                  ulonglong2 &st, float &dE)
     {
-        Prop q;
-        if (!kGauss) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const float re = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
-                const float im = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
-                q.w[k] = cmk(me.z[k].re + re, me.z[k].im + im);
-            }
-            q.dv = he3_potential_f(q.w, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d);
-        } else {
-#pragma unroll
-            for (int mu = 0; mu < 3; ++mu) {
-                q.w[2 * mu] = normal_pair(st);      // zp
-                q.w[2 * mu + 1] = normal_pair(st);  // zm
-            }
-            q.dv = 0.0f;
-        }
-        q.v = mcgb_fast_unit(xoro_next(st));
-        return q;
-    }
-    template <int C_>
-    static __device__ __forceinline__ bool decide(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *,
-                                                  const Prop &q, float &dE)
-    {
-        if (!kGauss) {
-            const float diff = q.dv + x.K * he3_grad_diff<C_>(nb, me, q.w);
-            if (diff <= 0.0f || q.v < __expf(-x.beta * diff)) {
-#pragma unroll
-                for (int k = 0; k < 6; ++k) me.z[k] = q.w[k];
-                dE = diff;
-                return true;
-            }
-            return false;
-        }
-        // gaussian_fast.py:26-40 neighbour field, :53-88 proposal and log ratio.
-        const He3Cell &R = MCGB_NBR(nb, kDown(C_));
-        const He3Cell &U = MCGB_NBR(nb, kRight(C_));
-        const He3Cell &Lf = MCGB_NBR(nb, kUp(C_));
-        const He3Cell &D = MCGB_NBR(nb, kLeft(C_));
-        const He3Cell &LU = MCGB_NBR(nb, kUpRight(C_));
-        const He3Cell &DR = MCGB_NBR(nb, kDownLeft(C_));
-        const float root = 0.7071067811865475f;
-        const float plus = 10.0f * x.K + x.mass, minus = 6.0f * x.K + x.mass;
-        const float vf = 1.0f - x.rho * x.rho;
-        const float sp = sqrtf(vf / (2.0f * x.beta * plus));
-        const float sm = sqrtf(vf / (2.0f * x.beta * minus));
-        const float qp = vf / (8.0f * root * root * sp * sp);
-        const float qm = vf / (8.0f * root * root * sm * sm);
-        c32 nxt[6];
-        float lpr = 0.0f;
-#pragma unroll
-        for (int mu = 0; mu < 3; ++mu) {
-            const int kx = 2 * mu, ky = 2 * mu + 1;
-            const c32 f0 = -3.0f * (R.z[kx] + Lf.z[kx]) - U.z[kx] - U.z[ky] - R.z[ky] - Lf.z[ky] - D.z[kx] -
-                           D.z[ky] + LU.z[ky] + DR.z[ky];
-            const c32 f1 = -R.z[kx] - R.z[ky] - U.z[kx] - Lf.z[kx] - Lf.z[ky] - D.z[kx] -
-                           3.0f * (U.z[ky] + D.z[ky]) + LU.z[kx] + DR.z[kx];
-            const c32 xo = me.z[kx], yo = me.z[ky];
-            const c32 hp = root * (f0 + f1), hm = root * (f0 - f1);
-            c32 mp = (-x.K) * hp, mm = (-x.K) * hm;
-            mp = cmk(mp.re / plus, mp.im / plus);
-            mm = cmk(mm.re / minus, mm.im / minus);
-            const c32 mx = root * (mp + mm), my = root * (mp - mm);
-            const c32 zp = sp * q.w[kx], zm = sm * q.w[ky];
-            const c32 nx = (mx + x.rho * (xo - mx)) + root * (zp + zm);
-            const c32 ny = (my + x.rho * (yo - my)) + root * (zp - zm);
-            nxt[kx] = nx;
-            nxt[ky] = ny;
-            const c32 op = (xo - mx) + (yo - my), om = (xo - mx) - (yo - my);
-            const c32 np = (nx - mx) + (ny - my), nm = (nx - mx) - (ny - my);
-            lpr += qp * (norm2(np) - norm2(op));
-            lpr += qm * (norm2(nm) - norm2(om));
-        }
-        const float dh = he3_potential_f(nxt, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d) +
-                         x.K * he3_grad_diff<C_>(nb, me, nxt);
-        const float log_ratio = -x.beta * dh + lpr;
-        if (!isfinite(log_ratio)) {
-            if (x.nonfinite) atomicAdd(reinterpret_cast<unsigned long long *>(x.nonfinite), 1ull);
-            return false;
-        }
-        if (log_ratio >= 0.0f || q.v < __expf(log_ratio)) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) me.z[k] = nxt[k];
-            dE = dh;
-            return true;
-        }
-        return false;
+        const He3Nbrs n{&MCGB_NBR(nb, kDown(C_)), &MCGB_NBR(nb, kRight(C_)), &MCGB_NBR(nb, kUp(C_)),
+                        &MCGB_NBR(nb, kLeft(C_)), &MCGB_NBR(nb, kUpRight(C_)), &MCGB_NBR(nb, kDownLeft(C_))};
+        const He3Visit v = he3_visit<kGauss>(x, n, &me, st);
+        st = v.st;
+        dE = v.dE;
+        return v.accepted != 0;
     }
     template <int C_>
     static __device__ __forceinline__ void measure(const Ctx &x, const Nbrs<Cell> &nb, const Cell &me, const float *,
@@ -608,7 +633,10 @@ int continuum_launch(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_
         const long long n = (long long)L * L / (4 * effective_cluster(L, w.cluster_size));
         if (n > npl) npl = n;
     }
-    if (npl <= w.threads) return launch_window<M, 1>(a, w, s, name);
+    // One plaquette a thread, or two with the streams still in registers;
+    // beyond that (or above the two-plaquette variant's thread bound) the
+    // one-plaquette variant keeps the streams in global memory.
+    if (npl <= w.threads || w.threads > window_max_threads<M, 2>()) return launch_window<M, 1>(a, w, s, name);
     return launch_window<M, 2>(a, w, s, name);
 }
 
@@ -639,6 +667,7 @@ template <class M>
 int continuum_clusters(int C, int threads, size_t smem, int *out)
 {
     MCGB_REQUIRE(threads <= M::kMaxThreads, "at most %d threads per CTA for this model", M::kMaxThreads);
+    if (threads > window_max_threads<M, 2>()) return max_clusters_for<M, 1>(C, threads, smem, out);
     return max_clusters_for<M, 2>(C, threads, smem, out);
 }
 

@@ -30,7 +30,9 @@ struct IsingPolicy {
     static constexpr int kChannels = 2;  // energy, magnetization
     static constexpr int kSums = 2;
     static constexpr int kMaxThreads = 1024;
+    static constexpr int kPairThreads = 512;
     static constexpr bool kSplitMiddle = false;
+    static constexpr bool kPipeline = true;
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
 
@@ -119,7 +121,9 @@ struct XYPolicy {
     static constexpr int kChannels = 5;   // energy, mx, my, twist_cos_x, twist_sin_x
     static constexpr int kSums = 5;
     static constexpr int kMaxThreads = 1024;
+    static constexpr int kPairThreads = 512;
     static constexpr bool kSplitMiddle = false;
+    static constexpr bool kPipeline = true;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 

@@ -44,6 +44,9 @@
 //   void store(const Args&, int64_t site, const Cell&, const float* own)
 //   Prop propose<c>(const Ctx&, const Cell&, const float* own, ulonglong2&)
 //   bool decide<c>(const Ctx&, Nbrs, Cell&, float* own, const Prop&, float& dE)
+// or, with kPipeline = false (no propose/decide split: every phase waits
+// first, then each visit draws and decides in one call),
+//   bool update<c>(const Ctx&, Nbrs, Cell&, float* own, ulonglong2&, float& dE)
 //   void measure<c>(const Ctx&, Nbrs, const Cell&, const float* own, FSum* v)
 //   void finish_sample(const Ctx&, double* v)  (turns kSums reduced sums, sum 0
 //        the energy, into the kChannels output channels, in place)
@@ -240,14 +243,47 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
         const Site s = make_site(p, g.LP);
         float *o = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
         typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
-        const typename M::Prop pr = M::template propose<C_>(ctx, me, o, sv);
-        rng_g[idx] = sv;
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
         float dE;
-        if (M::template decide<C_>(ctx, nb, me, o, pr, dE)) {
+        bool accepted;
+        if constexpr (M::kPipeline) {
+            const typename M::Prop pr = M::template propose<C_>(ctx, me, o, sv);
+            rng_g[idx] = sv;
+            accepted = M::template decide<C_>(ctx, nb, me, o, pr, dE);
+        } else {
+            accepted = M::template update<C_>(ctx, nb, me, o, sv, dE);
+            rng_g[idx] = sv;
+        }
+        if (accepted) {
             dacc += dE;
             ++nacc;
             push_halo<C_>(cells, g, s, me);
+        }
+    }
+}
+
+// A colour of a non-pipelined policy (kPipeline = false) with the streams in
+// registers: each visit draws and decides in one call, so nothing is held in
+// registers across a cluster barrier.
+template <class M, int NK, int C_>
+__device__ __forceinline__ void fused_pass(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
+                                           const StripCtx &g, const Site (&sites)[NK], ulonglong2 (&st)[NK][4],
+                                           float &dacc, int &nacc)
+{
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+        const int p = threadIdx.x + k * blockDim.x;
+        if (p < g.NPL) {
+            const Site &s = sites[k];
+            const Nbrs<typename M::Cell> nb{cells, g.PS, s};
+            typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
+            float dE;
+            if (M::template update<C_>(ctx, nb, me, own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, st[k][C_],
+                                       dE)) {
+                dacc += dE;
+                ++nacc;
+                push_halo<C_>(cells, g, s, me);
+            }
         }
     }
 }
@@ -342,9 +378,6 @@ __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typena
     }
 }
 
-// Threads per block the NPMAX variant is compiled for: NPMAX streams of four
-// colours live in registers (16 registers per plaquette); policies with large
-// cells cap it with kMaxThreads.
 // Fused exchange, run by the rank-0 CTA of a cluster after it finished
 // replica `rep`: the CTA that completes the ladder's last replica runs the
 // ladder's exchange (the classic last-block pattern: every finisher fences
@@ -380,10 +413,15 @@ __device__ __forceinline__ void launch_finished(const FusedExchange &fx, const W
     }
 }
 
+// Threads per block the NPMAX variant is compiled for: NPMAX streams of four
+// colours live in registers (16 registers per plaquette).  kMaxThreads caps
+// every variant, kPairThreads the two-plaquette one (its launch bound sets
+// the register budget: 256 threads leave 255 registers a thread).
 template <class M, int NPMAX>
 constexpr int window_max_threads()
 {
-    return (NPMAX <= 1 ? 1024 : 512) < M::kMaxThreads ? (NPMAX <= 1 ? 1024 : 512) : M::kMaxThreads;
+    return NPMAX <= 1 ? (1024 < M::kMaxThreads ? 1024 : M::kMaxThreads)
+                      : (M::kPairThreads < M::kMaxThreads ? M::kPairThreads : M::kMaxThreads);
 }
 
 template <class M, int NPMAX>
@@ -469,12 +507,31 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             combine_sample<M>(ctx, cm, parts, red, C, pend, r, tslot, e_hi0, e_lo0, a.n_replicas);          \
         pend = -1;                                                                                          \
     }
-        typename M::Prop pa[NK], pb[NK];
+        [[maybe_unused]] typename M::Prop pa[NK], pb[NK];
         for (int s = 0; s < cm.n_sweeps; ++s) {
             // This sweep's accepted energy changes (at most a few terms per
             // thread), folded into the compensated running sum once per sweep.
             float dacc = 0.0f;
-            if (regs) {
+            if (!M::kPipeline && regs) {
+                if constexpr (!M::kPipeline) {
+                    cluster_wait();
+                    MCGB_COMBINE_PENDING()
+                    fused_pass<M, NK, 0>(ctx, cells, own, g, sites, st, dacc, nacc);
+                    cluster_arrive();
+                    cluster_wait();
+                    fused_pass<M, NK, 1>(ctx, cells, own, g, sites, st, dacc, nacc);
+                    if (M::kSplitMiddle) {
+                        cluster_arrive();
+                        cluster_wait();
+                    }
+                    fused_pass<M, NK, 2>(ctx, cells, own, g, sites, st, dacc, nacc);
+                    cluster_arrive();
+                    cluster_wait();
+                    fused_pass<M, NK, 3>(ctx, cells, own, g, sites, st, dacc, nacc);
+                    cluster_arrive();
+                }
+            } else if (regs) {
+                if constexpr (M::kPipeline) {
                 // Invariant: this thread has arrived at the barrier that
                 // follows the previous phase and not yet waited.
                 propose_pass<M, NK, 0>(ctx, cells, own, g, sites, st, pa);
@@ -496,6 +553,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 cluster_wait();
                 decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 cluster_arrive();
+                }
             } else {
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
