@@ -222,7 +222,7 @@ struct KawamuraPolicy {
     }
     template <int C_>
     static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &, const Cell &, const float *,
-                                                       double &)
+                                                       FSum &)
     {
     }
     static __device__ __forceinline__ void finish_sample(const Ctx &, double *v)
@@ -511,7 +511,7 @@ struct He3Policy {
     }
     template <int C_>
     static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &, const Cell &, const float *,
-                                                       double &)
+                                                       FSum &)
     {
     }
     static __device__ __forceinline__ void finish_sample(const Ctx &, double *v)

@@ -104,9 +104,9 @@ struct IsingPolicy {
     }
     template <int C_>
     static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
-                                                       const float *, double &e)
+                                                       const float *, FSum &e)
     {
-        e += (double)(me * (MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kRight(C_))));
+        e += (float)(me * (MCGB_NBR(nb, kDown(C_)) + MCGB_NBR(nb, kRight(C_))));
     }
     static __device__ __forceinline__ void finish_sample(const Ctx &x, double *v) { v[0] *= -(double)x.J; }
     static __device__ __forceinline__ double finish_energy(const Ctx &x, double bonds) { return -(double)x.J * bonds; }
@@ -218,7 +218,7 @@ struct XYPolicy {
     }
     template <int C_>
     static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &, const Cell &,
-                                                       const float *, double &)
+                                                       const float *, FSum &)
     {
     }
     static __device__ __forceinline__ void finish_sample(const Ctx &, double *) {}

@@ -137,11 +137,21 @@ struct WindowCommon {
 constexpr int kRedDoubles = 16;  // per-CTA cluster reduction slots
 constexpr int kMaxCluster = 16;  // CTAs per cluster (non-portable maximum)
 
+// Partial sums a CTA pushes into rank 0: a sample's kSums, then the window
+// epilogue's three (energy change, acceptances, exact energy) in slots of
+// their own -- the epilogue's pushes may land while rank 0 still merges the
+// window's last sample.
+template <class M>
+__host__ __device__ constexpr int part_slots()
+{
+    return M::kSums + 3;
+}
+
 // Shared memory of a strip with npl plaquettes in rows of lp.
 template <class M>
 __host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp)
 {
-    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * M::kSums) +
+    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * part_slots<M>()) +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
            (size_t)4 * npl * sizeof(float) * M::kOwnFloats;
 }
@@ -321,7 +331,7 @@ __device__ __noinline__ void push_sample(const typename M::Ctx ctx, typename M::
     measure_colour<M, 3>(ctx, cells, own, g, v);
     block_fsum<NS>(v, scratch);
     if (threadIdx.x == 0) {
-        float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NS;
+        float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * part_slots<M>();
 #pragma unroll
         for (int q = 0; q < NS; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
     }
@@ -342,7 +352,7 @@ __device__ __noinline__ void combine_sample(const typename M::Ctx ctx, const Win
     if (lane < NS) {
         FSum f;
         for (int k = 0; k < C; ++k) {
-            const float2 q = parts[k * NS + lane];
+            const float2 q = parts[k * part_slots<M>() + lane];
             f.merge(q.x, q.y);
         }
         red[lane] = f.value();
@@ -368,7 +378,7 @@ __device__ __noinline__ void combine_sample(const typename M::Ctx ctx, const Win
 
 template <class M, int C_>
 __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
-                                              const StripCtx &g, double &e)
+                                              const StripCtx &g, FSum &e)
 {
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
         const Site s = make_site(p, g.LP);
@@ -440,8 +450,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     extern __shared__ __align__(16) unsigned char smem[];
     double *red = reinterpret_cast<double *>(smem);  // kRedDoubles
     double *scratch = red + kRedDoubles;               // 32 * (NS + 3)
-    float2 *parts = reinterpret_cast<float2 *>(scratch + 32 * (NS + 3));  // [kMaxCluster][NS], rank 0's used
-    Cell *cells = reinterpret_cast<Cell *>(parts + kMaxCluster * NS);
+    constexpr int NP = part_slots<M>();
+    float2 *parts = reinterpret_cast<float2 *>(scratch + 32 * (NS + 3));  // [kMaxCluster][NP], rank 0's used
+    Cell *cells = reinterpret_cast<Cell *>(parts + kMaxCluster * NP);
 
     const WindowCommon &cm = a.c;
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
@@ -587,19 +598,23 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         MCGB_COMBINE_PENDING()
 #undef MCGB_COMBINE_PENDING
 
-        // Window epilogue: energy and acceptance bookkeeping, write back.
-        double v2[3] = {(double)dsum + (double)dcomp, (double)nacc, 0.0};
+        // Window epilogue: energy and acceptance bookkeeping (compensated
+        // float32 partial sums pushed into rank 0, as for samples), write back.
+        FSum v2[3];
+        v2[0].hi = dsum;
+        v2[0].lo = dcomp;
+        v2[1].hi = (float)nacc;  // exact: a thread's count is far below 2^24
         if (M::kExactEnergy) {
             energy_colour<M, 0>(ctx, cells, own, g, v2[2]);
             energy_colour<M, 1>(ctx, cells, own, g, v2[2]);
             energy_colour<M, 2>(ctx, cells, own, g, v2[2]);
             energy_colour<M, 3>(ctx, cells, own, g, v2[2]);
         }
-        block_sum<3>(v2, scratch);
+        block_fsum<3>(v2, reinterpret_cast<float2 *>(scratch));
         if (tid == 0) {
-            red[NS] = v2[0];
-            red[NS + 1] = v2[1];
-            red[NS + 2] = v2[2];
+            float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NP + NS;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) dst[q] = make_float2(v2[q].hi, v2[q].lo);
         }
         for (int c = 0; c < 4; ++c)
             for (int p = tid; p < g.NPL; p += T) {
@@ -618,32 +633,30 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         }
         cluster.sync();
         if (rank == 0 && tid == 0) {
-            double de = 0.0, na = 0.0, ex = 0.0;
+            FSum de, na, ex;
             for (int k = 0; k < C; ++k) {
-                const double *rr = cluster.map_shared_rank(red, k);
-                de += rr[NS];
-                na += rr[NS + 1];
-                ex += rr[NS + 2];
+                const float2 *pk = parts + k * NP + NS;
+                de.merge(pk[0].x, pk[0].y);
+                na.merge(pk[1].x, pk[1].y);
+                ex.merge(pk[2].x, pk[2].y);
             }
             float hi, lo2;
             if (M::kExactEnergy) {
-                const double e = M::finish_energy(ctx, ex);
+                const double e = M::finish_energy(ctx, ex.value());
                 hi = (float)e;
                 lo2 = (float)(e - (double)hi);
                 cm.energies[r] = e;
             } else {
                 // Compensated (hi, lo) float update of the running energy.
-                const float de_hi = (float)de;
-                const float de_lo = (float)(de - (double)de_hi);
                 float s1, e1;
-                two_sum(e_hi0, de_hi, s1, e1);
-                const float lo = e_lo0 + e1 + de_lo;
+                two_sum(e_hi0, de.hi, s1, e1);
+                const float lo = e_lo0 + e1 + de.lo;
                 two_sum(s1, lo, hi, lo2);
                 cm.energies[r] = (double)hi + (double)lo2;
             }
             cm.e_run[2 * r] = hi;
             cm.e_run[2 * r + 1] = lo2;
-            cm.accepted[r] += (long long)na;
+            cm.accepted[r] += (long long)na.value();
         }
         cluster.sync();
         if (a.fx.enabled && rank == 0) ladder_finished(a.fx, rep);
