@@ -366,8 +366,9 @@ def run_mcgb(args, rank, world):
 
     # Plain FP64 form on the same ladder (one lattice per launch), bounded.
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
-    # One fused launch per window: sweeps, per-ladder exchange, clock tick.
-    launches = args.steps * (SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
+    # A resident launch runs a whole step (10 windows with their exchanges);
+    # otherwise one fused launch per window.
+    launches = args.steps * (1 if batch.resident else SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
 
     line = None
     if rank == 0:
@@ -379,7 +380,8 @@ def run_mcgb(args, rank, world):
             "config": {"workload": WORKLOAD, "L": L, "replicas_per_gpu": N_TEMPS,
                        "sweeps_per_step": SWEEPS_PER_STEP, "exchange_interval": EXCHANGE_INTERVAL,
                        "sample_interval": SAMPLE_INTERVAL, "cluster_size": batch.cluster_size,
-                       "threads": batch.threads, "l2": "flushed (256 MB write) between timed steps",
+                       "threads": batch.threads, "resident_launch": bool(batch.resident),
+                       "l2": "flushed (256 MB write) between timed steps",
                        "parallelism": f"independent ladders x{world}"},
             "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
@@ -623,7 +625,7 @@ def run_workload(args, rank, world):
                      "traffic": None, "kernel": f"window_kernel ({kind})", "kernel_ms": window_ms,
                      "bytes_per_update": BYTES[kind], "peak_source": peak_kind},
         "clocks": clk,
-        "gpu_launches": args.steps * windows_per_step * (1 if ex else 2),
+        "gpu_launches": args.steps * (1 if (ex and batch.resident) else windows_per_step * (1 if ex else 2)),
     }
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1

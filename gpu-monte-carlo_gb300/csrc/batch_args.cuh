@@ -165,14 +165,27 @@ int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s
     cfg.blockDim = dim3((unsigned)w.threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)w.cluster_size;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cuda_status(cudaLaunchKernelEx(&cfg, kern, a), name);
+    if (a.fx.enabled && a.fx.n_windows > 1) {
+        // A resident launch's clusters wait for one another between windows:
+        // a cooperative launch guarantees they are all resident at once (or
+        // fails to launch).
+        attr[1].id = cudaLaunchAttributeCooperative;
+        attr[1].val.cooperative = 1;
+        cfg.numAttrs = 2;
+    }
+    const cudaError_t err = cudaLaunchKernelEx(&cfg, kern, a);
+    // A launch refused for its configuration (e.g. a cooperative grid too
+    // large to be resident) is not sticky: clear it so later checks do not
+    // report it again.
+    if (err != cudaSuccess) (void)cudaGetLastError();
+    return cuda_status(err, name);
 }
 
 template <class M, int NPMAX>

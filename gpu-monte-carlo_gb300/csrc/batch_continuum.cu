@@ -66,7 +66,9 @@ struct KawamuraPolicy {
 
     static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
     {
-        return Ctx{a.c.betas[r], a.J, a.delta, kGauss ? a.sigma_t[rep.ladder_start + a.c.w2t[r]] : 0.0f};
+        // betas and the map are rewritten by exchanges within a resident launch
+        return Ctx{__ldcg(a.c.betas + r), a.J, a.delta,
+                   kGauss ? __ldcg(a.sigma_t + rep.ladder_start + __ldcg(a.c.w2t + r)) : 0.0f};
     }
     // A pair of standard normals from one draw (Box-Muller, fast intrinsics).
     static __device__ __forceinline__ float2 normal_pair(uint64_t bits)
@@ -439,7 +441,7 @@ struct He3Policy {
     static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
     {
         Ctx x;
-        x.beta = a.c.betas[r];
+        x.beta = __ldcg(a.c.betas + r);  // rewritten by exchanges within a resident launch
         x.K = a.K;
         x.delta = a.delta;
         x.g_d = a.g_d;

@@ -28,15 +28,17 @@ struct ExchangeArgs {
     long long first_sample_sweep;
 };
 
-// Every thread of the block calls this with the same l.  Energies and staged
-// samples may have been written by other CTAs of the same launch (the fused
-// path orders them with a fence before its completion count), so they are
-// read past L1.
+// Every thread of the block calls this with the same l.  Everything it reads
+// may have been written earlier in the same launch by another CTA (the
+// energies and staged samples of this window; in a resident launch, the maps,
+// counters and streams of the previous window's exchange, which another CTA
+// may have run), ordered by fences and completion counts: so every read goes
+// past L1 (ld.global.cg).
 __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
 {
     const int start = x.starts[l], R = x.sizes[l];
-    const long long sweep = x.clock[0] + x.window_sweeps;
-    const int parity = R > 2 ? (int)(x.clock[1] & 1) : 0;
+    const long long sweep = __ldcg(x.clock) + x.window_sweeps;
+    const int parity = R > 2 ? (int)(__ldcg(x.clock + 1) & 1) : 0;
     const int poff = start - l;
     const double *E = x.energies + start;
     float *B = x.betas + start;
@@ -45,15 +47,16 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
               *nonfinite = x.counts + 2 * x.n_pairs_total + poff;
     for (int left = parity + 2 * (int)threadIdx.x; left < R - 1; left += 2 * blockDim.x) {
         const int right = left + 1;
-        const int a = T2W[left], b = T2W[right];
+        const int a = __ldcg(T2W + left), b = __ldcg(T2W + right);
         const double ea = __ldcg(E + a), eb = __ldcg(E + b);
-        attempts[left] += 1;
+        attempts[left] = __ldcg(attempts + left) + 1;
         if (!isfinite(ea) || !isfinite(eb)) {
-            nonfinite[left] += 1;
+            nonfinite[left] = __ldcg(nonfinite + left) + 1;
             continue;
         }
-        const double log_ratio = ((double)B[a] - (double)B[b]) * (ea - eb);
-        ulonglong2 st = x.rng[poff + left];
+        const float ba = __ldcg(B + a), bb = __ldcg(B + b);
+        const double log_ratio = ((double)ba - (double)bb) * (ea - eb);
+        ulonglong2 st = __ldcg(x.rng + poff + left);
         const double u = xoro_uniform_f64(st);
         x.rng[poff + left] = st;
         if (log_ratio >= 0.0 || u == 0.0 || log(u) < log_ratio) {
@@ -61,10 +64,9 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
             T2W[right] = a;
             W2T[a] = right;
             W2T[b] = left;
-            const float ba = B[a];
-            B[a] = B[b];
+            B[a] = bb;
             B[b] = ba;
-            accepted[left] += 1;
+            accepted[left] = __ldcg(accepted + left) + 1;
         }
     }
     __syncthreads();
@@ -72,17 +74,17 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
     long long *origin = x.trips + start, *visited = x.trips + n + start, *sweep0 = x.trips + 2 * n + start,
               *ntrips = x.trips + 3 * n + start, *tsweeps = x.trips + 4 * n + start;
     for (int wk = threadIdx.x; wk < R; wk += blockDim.x) {
-        const int t = W2T[wk];
+        const int t = __ldcg(W2T + wk);
         if (t != 0 && t != R - 1) continue;
-        const long long o = origin[wk];
+        const long long o = __ldcg(origin + wk);
         if (o < 0) {
             origin[wk] = t;
             sweep0[wk] = sweep;
         } else if (t != o) {
             visited[wk] = 1;
-        } else if (visited[wk]) {
-            ntrips[wk] += 1;
-            tsweeps[wk] += sweep - sweep0[wk];
+        } else if (__ldcg(visited + wk)) {
+            ntrips[wk] = __ldcg(ntrips + wk) + 1;
+            tsweeps[wk] = __ldcg(tsweeps + wk) + (sweep - __ldcg(sweep0 + wk));
             sweep0[wk] = sweep;
             visited[wk] = 0;
         }
@@ -91,7 +93,7 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
         const int slot = sample_slot(sweep, x.first_sample_sweep, x.sample_interval, x.n_slots);
         if (slot >= 0) {
             for (int wk = threadIdx.x; wk < R; wk += blockDim.x) {
-                const int dst = start + W2T[wk];
+                const int dst = start + __ldcg(W2T + wk);
                 for (int q = 0; q < x.channels; ++q)
                     x.samples[((size_t)slot * x.channels + q) * x.n_temps_total + dst] =
                         __ldcg(x.staging + (size_t)q * n + start + wk);
@@ -102,12 +104,17 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
 }
 
 // Completion bookkeeping of the fused window + exchange launch.  `sync` holds
-// one counter per ladder and one for the launch, all zero between launches.
+// one counter per ladder, one for the launch, the resident launch's window
+// epoch and its error flag; the counters and the epoch are zero between
+// launches.
 struct FusedExchange {
     ExchangeArgs ex;
     int32_t *ladder_done;  // [n_ladders]
     int32_t *launch_done;  // [1]
+    int32_t *epoch;        // [1] resident launches: windows completed so far
+    int32_t *error;        // [1] set when a wait for the epoch gave up
     int enabled;
+    int n_windows;         // > 1: a resident launch (one replica per cluster, cooperative)
 };
 
 }  // namespace mcgb

@@ -51,7 +51,7 @@ struct IsingPolicy {
     {
         Ctx x;
         x.J = a.J;
-        const float beta = a.c.betas[r];
+        const float beta = __ldcg(a.c.betas + r);  // rewritten by exchanges within a resident launch
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
             const float dE = (float)(4 * q - 8) * a.J;
@@ -139,11 +139,11 @@ struct XYPolicy {
     static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
     {
         Ctx x;
-        x.beta = a.c.betas[r];
+        x.beta = __ldcg(a.c.betas + r);  // rewritten by exchanges within a resident launch
         x.J = a.J;
         x.delta = a.delta;
         x.gauss = a.sigma_t != nullptr;
-        x.sigma = x.gauss ? a.sigma_t[rep.ladder_start + a.c.w2t[r]] : 0.0f;
+        x.sigma = x.gauss ? __ldcg(a.sigma_t + rep.ladder_start + __ldcg(a.c.w2t + r)) : 0.0f;
         return x;
     }
     // The (cos, sin) cache persists in `aux` between windows, so the chain

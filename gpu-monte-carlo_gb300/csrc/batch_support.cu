@@ -169,7 +169,35 @@ extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w,
     fx.ex = make_exchange_args(*w, *pt);
     fx.ladder_done = sync;
     fx.launch_done = sync + pt->n_ladders;
+    fx.epoch = nullptr;
+    fx.error = nullptr;
     fx.enabled = 1;
+    fx.n_windows = 1;
+    return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
+                             : continuum_window(model, *w, as_stream(stream), &fx);
+}
+
+extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
+                                       int32_t *sync, int n_windows, void *stream)
+{
+    MCGB_REQUIRE(known_model(model), "unknown model %d", model);
+    MCGB_REQUIRE(w && pt, "run_resident: null argument block");
+    MCGB_REQUIRE(sync != nullptr, "run_resident: null sync counters");
+    MCGB_REQUIRE(n_windows >= 1, "run_resident: n_windows must be >= 1");
+    MCGB_REQUIRE(n_windows == 1 || w->n_clusters == w->n_replicas,
+                 "run_resident: a resident launch needs one cluster per replica (n_clusters == n_replicas)");
+    if (int st = check_exchange(*w, *pt)) return st;
+    if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
+    if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
+    if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
+    FusedExchange fx;
+    fx.ex = make_exchange_args(*w, *pt);
+    fx.ladder_done = sync;
+    fx.launch_done = sync + pt->n_ladders;
+    fx.epoch = sync + pt->n_ladders + 1;
+    fx.error = sync + pt->n_ladders + 2;
+    fx.enabled = 1;
+    fx.n_windows = n_windows;
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
 }

@@ -409,17 +409,59 @@ __device__ __forceinline__ void ladder_finished(const FusedExchange &fx, const m
 
 // After a cluster's whole work list (thread 0 of its rank-0 CTA): the last
 // cluster to finish advances the device clock, after every ladder's exchange
-// has read it, and resets the launch counter.
+// has read it, and resets the launch counter (and a resident launch's epoch).
 __device__ __forceinline__ void launch_finished(const FusedExchange &fx, const WindowCommon &cm, int n_clusters)
 {
     __threadfence();
     if (atomicAdd(fx.launch_done, 1) == n_clusters - 1) {
         __threadfence();
         long long *clock = const_cast<long long *>(cm.clock);
-        clock[0] += cm.n_sweeps;
-        clock[1] += 1;
+        clock[0] = __ldcg(clock) + cm.n_sweeps;
+        clock[1] = __ldcg(clock + 1) + 1;
+        *fx.launch_done = 0;
+        if (fx.n_windows > 1) *fx.epoch = 0;
+        __threadfence();
+    }
+}
+
+__device__ __forceinline__ int load_acquire(const int32_t *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Iterations of the epoch wait (each sleeps 32..256 ns) before a resident
+// launch gives up: ~1 s, far beyond a window's length.
+constexpr long long kEpochSpinLimit = 1ll << 22;
+
+// Between two windows of a resident launch (thread 0 of each cluster's rank-0
+// CTA, after its ladder bookkeeping): count the cluster; the last one
+// advances the clock, resets the count and publishes window `win` as done;
+// every cluster then waits for that epoch.  All clusters are co-resident (a
+// cooperative launch), so the wait ends; it is bounded all the same: on
+// giving up it raises the error flag and goes on (the host reports it).
+__device__ __forceinline__ void window_finished(const FusedExchange &fx, const WindowCommon &cm, int n_clusters,
+                                                int win)
+{
+    __threadfence();
+    if (atomicAdd(fx.launch_done, 1) == n_clusters - 1) {
+        __threadfence();
+        long long *clock = const_cast<long long *>(cm.clock);
+        clock[0] = __ldcg(clock) + cm.n_sweeps;
+        clock[1] = __ldcg(clock + 1) + 1;
         *fx.launch_done = 0;
         __threadfence();
+        atomicExch(fx.epoch, win + 1);
+    }
+    unsigned ns = 32;
+    for (long long it = 0; load_acquire(fx.epoch) < win + 1; ++it) {
+        if (it >= kEpochSpinLimit) {
+            atomicExch(fx.error, 1);
+            break;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
     }
 }
 
@@ -475,7 +517,6 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         const int64_t gplane = (int64_t)g.LP * g.LP;
         const int64_t base = rep.state_offset + (int64_t)rank * g.NPL;
 
-        const typename M::Ctx ctx = M::prepare(a, r, rep);
         // Load the strip; boundary rows also go to the neighbours' halos.
         for (int c = 0; c < 4; ++c)
             for (int p = tid; p < g.NPL; p += T) {
@@ -502,9 +543,15 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                     if (p < g.NPL) st[k][c] = rng_g[base + c * gplane + p];
             }
         }
-        const float e_hi0 = cm.e_run[2 * r], e_lo0 = cm.e_run[2 * r + 1];
-        const long long sweep0 = cm.clock[0];
-        const int tslot = rep.ladder_start + cm.w2t[r];
+        // A resident launch runs n_windows windows with the strip on chip,
+        // exchanging (and waiting for every cluster) between them; values the
+        // exchange rewrites are re-read past L1 at each window start.
+        const int n_windows = a.fx.enabled && a.fx.n_windows > 1 ? a.fx.n_windows : 1;
+        for (int win = 0; win < n_windows; ++win) {
+        const typename M::Ctx ctx = M::prepare(a, r, rep);
+        const float e_hi0 = __ldcg(cm.e_run + 2 * r), e_lo0 = __ldcg(cm.e_run + 2 * r + 1);
+        const long long sweep0 = __ldcg(cm.clock);
+        const int tslot = rep.ladder_start + __ldcg(cm.w2t + r);
         cluster_arrive();
 
         float dsum = 0.0f, dcomp = 0.0f;
@@ -616,6 +663,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
 #pragma unroll
             for (int q = 0; q < 3; ++q) dst[q] = make_float2(v2[q].hi, v2[q].lo);
         }
+        if (win + 1 == n_windows) {
         for (int c = 0; c < 4; ++c)
             for (int p = tid; p < g.NPL; p += T) {
                 const Site s = make_site(p, g.LP);
@@ -630,6 +678,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 for (int c = 0; c < 4; ++c)
                     if (p < g.NPL) rng_g[base + c * gplane + p] = st[k][c];
             }
+        }
         }
         cluster.sync();
         if (rank == 0 && tid == 0) {
@@ -656,10 +705,16 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
             cm.e_run[2 * r] = hi;
             cm.e_run[2 * r + 1] = lo2;
-            cm.accepted[r] += (long long)na.value();
+            cm.accepted[r] = __ldcg(cm.accepted + r) + (long long)na.value();
         }
         cluster.sync();
         if (a.fx.enabled && rank == 0) ladder_finished(a.fx, rep);
+        if (win + 1 < n_windows) {
+            if (rank == 0 && tid == 0) window_finished(a.fx, cm, (int)(gridDim.x / C), win);
+            __syncwarp();  // the aligned cluster barrier needs warp 0 converged again
+            cluster.sync();
+        }
+        }  // windows
     }
     if (a.fx.enabled && rank == 0 && tid == 0) launch_finished(a.fx, cm, (int)(gridDim.x / C));
 }

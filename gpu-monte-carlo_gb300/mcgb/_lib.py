@@ -55,6 +55,7 @@ SIGNATURES = {
     "mcgb_batch_recompute_energy": [_I, _P, _P, _P],
     "mcgb_batch_exchange": [_P, _P, _P],
     "mcgb_batch_window_exchange": [_I, _P, _P, _P, _P],
+    "mcgb_batch_run_resident": [_I, _P, _P, _P, _I, _P],
     "mcgb_batch_clock_tick": [_P, _I, _I, _P],
     "mcgb_batch_tune_sigma": [_P, _P, _P, _P, _P, _I, _I, _F, _F, _F, _F, _P],
     "mcgb_batch_window_exchange_noalloc": [_I, _P, _P, _P],

@@ -142,8 +142,10 @@ class LadderBatch:
 
     def __init__(self, model, ladders, seeds=None, exchange_interval=10, exchange_seeds=None,
                  proposal="uniform", sigma0=1.0, gaussian=False, rho=-0.9, proposal_mass=0.0,
-                 cluster_size=None, threads=None, initial_states=None):
+                 cluster_size=None, threads=None, initial_states=None, resident=True):
         self.model = model
+        self._resident_wanted = bool(resident)
+        self._resident_checked = False
         self.model_id, self.dtype, self.site_shape = _model_info(model, gaussian, proposal)
         self.channels = CHANNELS[self.model_id]
         self.pt = exchange_interval is not None
@@ -246,8 +248,9 @@ class LadderBatch:
                 pair_rng[po:po + n - 1].raw().copy_(sub.raw())
             self.pair_rng = pair_rng
             self.swap_counts = device_zeros((3, n_pairs), np.int64)
-            # Completion counters of the fused window + exchange launch.
-            self.sync = device_zeros(n_l + 1, np.int32)
+            # Completion counters of the fused window + exchange launch, then
+            # the resident launch's window epoch and its error flag.
+            self.sync = device_zeros(n_l + 3, np.int32)
             trips = np.zeros((5, self.R), np.int64)
             trips[0] = -1
             trips[2] = -1
@@ -396,6 +399,11 @@ class LadderBatch:
         self.n_clusters = min(m, self.R)
         wp, wi, _ = lpt_work_lists(self._costs(self.cluster_size), self.n_clusters)
         self.work_ptr, self.work_idx = to_device(wp), to_device(wi)
+        # Resident launches (many windows per launch, strips kept on chip)
+        # need one replica per cluster and every cluster resident at once.
+        self.resident = (self._resident_wanted and self.pt and self.n_clusters == self.R
+                         and bool(np.all(np.diff(wp) == 1)))
+        self._resident_checked = False
         self._graphs.clear()
 
     # ------------------------------------------------------------ argument blocks
@@ -494,7 +502,10 @@ class LadderBatch:
                     j += 1
                 remaining = j - i
                 while remaining:
-                    chunk = 1 << min(6, remaining.bit_length() - 1)
+                    if self.resident and full[1] and not tune:
+                        chunk = min(64, remaining)  # one resident launch
+                    else:
+                        chunk = 1 << min(6, remaining.bit_length() - 1)
                     self._replay(chunk, full, tune)
                     remaining -= chunk
                 i = j
@@ -509,18 +520,51 @@ class LadderBatch:
         if exchanged:
             self.exchange_rounds += times
 
+    def _enqueue_resident(self, n_sweeps, count):
+        s = _lib.stream_handle()
+        w = self._window(n_sweeps, staging=True)
+        p = self._pt()
+        self._keep, self._keep_pt = w, p
+        _lib.call("mcgb_batch_run_resident", self.model_id, ctypes.byref(w), ctypes.byref(p), self.sync.cptr,
+                  int(count), s)
+
     def _replay(self, count, step, tune):
-        key = (count, step, tune, self.samples is not None and self.samples.ptr)
+        resident = self.resident and step[1] and not tune and count > 1
+        if resident and not self._resident_checked:
+            # First resident launch runs directly: if this device cannot hold
+            # every cluster at once the cooperative launch fails before doing
+            # anything, and the batch falls back to one launch per window.
+            try:
+                self._enqueue_resident(step[0], count)
+                self._resident_checked = True
+                self._advance(step[0], step[1], count)
+                return
+            except _lib.MCGBError:
+                self.resident, resident = False, False
+        key = (count, step, tune, self.samples is not None and self.samples.ptr, resident)
         g = self._graphs.get(key)
         if g is None:
             # Capture reads only argument blocks; the device clock advances at replay.
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
-                for _ in range(count):
-                    self._enqueue_window(step[0], step[1], tune)
+                if resident:
+                    self._enqueue_resident(step[0], count)
+                else:
+                    for _ in range(count):
+                        self._enqueue_window(step[0], step[1], tune)
             self._graphs[key] = g
         g.replay()
         self._advance(step[0], step[1], count)
+
+    def check_errors(self):
+        """Raise MCGBTimeout if a resident launch gave up waiting between
+        windows (its results are then unreliable); clears the flag."""
+        if not self.pt:
+            return
+        flag = self.sync.copy_to_host()[-1]
+        if flag:
+            self.sync.copy_to_device(np.zeros(len(self.ladders) + 3, np.int32))
+            raise _lib.MCGBTimeout(-4, "a resident launch timed out waiting between windows")
 
     def exchange_now(self):
         """Attempt one matching now (fresh energies from the running cache)."""
@@ -626,6 +670,7 @@ class LadderBatch:
         self.allocate_samples(start + thermalization_sweeps + sample_interval, sample_interval, n_slots)
         self.run(measurement_sweeps, tune=False, graph=graph)
         data = self.samples.copy_to_host()
+        self.check_errors()
         sample_sweeps = thermalization_sweeps + sample_interval * np.arange(1, n_slots + 1)
         runs = []
         for k, (L, T) in enumerate(self.ladders):

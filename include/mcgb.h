@@ -306,6 +306,19 @@ int mcgb_batch_window_exchange_noalloc(int model, const mcgb_batch_window *w, co
  * sharing a `sync` array must not overlap on the GPU. */
 int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                int32_t *sync, void *stream);
+/* No counterpart in the reference.  n_windows consecutive windows of
+ * w->n_sweeps sweeps, each followed by every ladder's exchange and a clock
+ * tick, in ONE cooperative launch that keeps every strip, its halos and its
+ * RNG streams on chip between windows (loaded once, written back once).
+ * Needs one cluster per replica (w->n_clusters == w->n_replicas, one replica
+ * in every work list) and every cluster resident at once: otherwise the
+ * launch fails (a CUDA error, MCGB_ECUDA) and nothing runs.  `sync` is
+ * n_ladders + 3 int32: the counters of mcgb_batch_window_exchange, the window
+ * epoch, and an error flag the kernel sets (and leaves set) if a wait between
+ * windows gave up after about a second -- check it after the run.
+ * n_windows = 1 is mcgb_batch_window_exchange. */
+int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
+                            int32_t *sync, int n_windows, void *stream);
 /* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
  * a captured graph of windows and exchanges can be replayed. */
 int mcgb_batch_clock_tick(int64_t *clock, int n_sweeps, int exchanged, void *stream);
