@@ -568,7 +568,8 @@ def run_workload(args, rank, world):
     value = aggregate_rate(world, updates_per_step, args.steps, total_ms)
 
     # The window kernel alone (one window of the schedule, samples on).
-    win = ex or 10
+    from mcgb.batch import NO_EXCHANGE_WINDOW
+    win = ex or NO_EXCHANGE_WINDOW
     w = batch._window(win)
     _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
     torch.cuda.synchronize()
@@ -667,7 +668,8 @@ def profile_windows(cluster_size=4, threads=1024, workload="xy-pt-l128"):
         b = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
                         proposal="gaussian" if kind in ("xy", "kawamura-gauss") else "uniform",
                         gaussian=kind == "he3", cluster_size=cluster_size, threads=threads, initial_states=inits)
-        win = ex or 10
+        from mcgb.batch import NO_EXCHANGE_WINDOW
+        win = ex or NO_EXCHANGE_WINDOW
     w = b._window(win)
     for _ in range(6):
         _lib.call("mcgb_batch_window_run", b.model_id, ctypes.byref(w), _lib.stream_handle())

@@ -34,11 +34,134 @@ struct ExchangeArgs {
 // counters and streams of the previous window's exchange, which another CTA
 // may have run), ordered by fences and completion counts: so every read goes
 // past L1 (ld.global.cg).
+// Ladders of at most 32 temperatures: one warp, walker `lane` per lane.  All
+// reads go out in one round trip; each pair's left lane decides, and the
+// maps, betas, round-trip bookkeeping and the staged sample follow from the
+// decisions by shuffles.  The same result as the general path below, with
+// one memory round trip on the critical path instead of five.
+constexpr int kWarpLadderChannels = 16;
+
+__device__ __forceinline__ void exchange_ladder_warp(const ExchangeArgs &x, int l, int start, int R,
+                                                     long long sweep, int parity)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int poff = start - l, n = x.n_replicas, np = x.n_pairs_total;
+    const bool in = lane < R;
+    // Slot roles: a left slot starts a pair of this round's matching.
+    const bool left = in && lane >= parity && ((lane - parity) & 1) == 0 && lane < R - 1;
+    const bool right = in && lane >= 1 + parity && ((lane - 1 - parity) & 1) == 0;
+
+    // -- the one round of loads --
+    const int t2w = in ? __ldcg(x.t2w + start + lane) : 0;       // walker at slot `lane`
+    const int s = in ? __ldcg(x.w2t + start + lane) : 0;         // slot of walker `lane`
+    const double e = in ? __ldcg(x.energies + start + lane) : 0.0;
+    const float b = in ? __ldcg(x.betas + start + lane) : 0.0f;
+    long long att = 0, acc = 0, nonf = 0;
+    ulonglong2 st = make_ulonglong2(0, 0);
+    if (left) {
+        att = __ldcg(x.counts + poff + lane);
+        acc = __ldcg(x.counts + np + poff + lane);
+        nonf = __ldcg(x.counts + 2 * np + poff + lane);
+        st = __ldcg(x.rng + poff + lane);
+    }
+    long long *tr = x.trips + start + lane;
+    long long origin = 0, visited = 0, sweep0 = 0, ntrips = 0, tsweeps = 0;
+    if (in) {
+        origin = __ldcg(tr);
+        visited = __ldcg(tr + n);
+        sweep0 = __ldcg(tr + 2 * n);
+        ntrips = __ldcg(tr + 3 * n);
+        tsweeps = __ldcg(tr + 4 * n);
+    }
+    const bool scatter = x.staging != nullptr && x.samples != nullptr;
+    const int slot = scatter ? sample_slot(sweep, x.first_sample_sweep, x.sample_interval, x.n_slots) : -1;
+    double stg[kWarpLadderChannels];
+#pragma unroll
+    for (int q = 0; q < kWarpLadderChannels; ++q)
+        stg[q] = (in && slot >= 0 && q < x.channels) ? __ldcg(x.staging + (size_t)q * n + start + lane) : 0.0;
+
+    // -- decisions (left lanes), as in the general path --
+    const int bw = __shfl_sync(full, t2w, (lane + 1) & 31);
+    const double ea = __shfl_sync(full, e, t2w & 31), eb = __shfl_sync(full, e, bw & 31);
+    const float ba = __shfl_sync(full, b, t2w & 31), bb = __shfl_sync(full, b, bw & 31);
+    int swapped = 0;
+    if (left) {
+        att += 1;
+        if (!isfinite(ea) || !isfinite(eb)) {
+            nonf += 1;
+        } else {
+            const double log_ratio = ((double)ba - (double)bb) * (ea - eb);
+            const double u = xoro_uniform_f64(st);
+            if (log_ratio >= 0.0 || u == 0.0 || log(u) < log_ratio) {
+                swapped = 1;
+                acc += 1;
+            }
+        }
+    }
+
+    // -- new maps and betas --
+    const int sw_prev = __shfl_sync(full, swapped, (lane + 31) & 31);
+    const int t2w_prev = __shfl_sync(full, t2w, (lane + 31) & 31);
+    int t2w_new = t2w;
+    if (left && swapped) t2w_new = bw;
+    if (right && sw_prev) t2w_new = t2w_prev;
+    // walker `lane` sits at slot s: its pair starts at s (left) or s - 1 (right)
+    const bool s_left = s >= parity && ((s - parity) & 1) == 0 && s < R - 1;
+    const bool s_right = s >= 1 + parity && ((s - 1 - parity) & 1) == 0;
+    const int q0 = s_left ? s : (s_right ? s - 1 : 0);
+    const int swq = __shfl_sync(full, swapped, q0 & 31);
+    const int partner_slot = s_left ? s + 1 : (s_right ? s - 1 : s);
+    const int partner = __shfl_sync(full, t2w, partner_slot & 31);
+    const float b_partner = __shfl_sync(full, b, partner & 31);
+    const bool moved = in && (s_left || s_right) && swq;
+    const int w2t_new = moved ? (s_left ? s + 1 : s - 1) : s;
+    const float b_new = moved ? b_partner : b;
+
+    // -- stores --
+    if (in) {
+        x.t2w[start + lane] = t2w_new;
+        x.w2t[start + lane] = w2t_new;
+        x.betas[start + lane] = b_new;
+    }
+    if (left) {
+        x.counts[poff + lane] = att;
+        x.counts[np + poff + lane] = acc;
+        x.counts[2 * np + poff + lane] = nonf;
+        x.rng[poff + lane] = st;
+    }
+    if (in && (w2t_new == 0 || w2t_new == R - 1)) {
+        const int t = w2t_new;
+        if (origin < 0) {
+            tr[0] = t;
+            tr[2 * n] = sweep;
+        } else if (t != origin) {
+            tr[n] = 1;
+        } else if (visited) {
+            tr[3 * n] = ntrips + 1;
+            tr[4 * n] = tsweeps + (sweep - sweep0);
+            tr[2 * n] = sweep;
+            tr[n] = 0;
+        }
+    }
+    if (in && slot >= 0) {
+        double *out = x.samples + (size_t)slot * x.channels * x.n_temps_total + start + w2t_new;
+#pragma unroll
+        for (int q = 0; q < kWarpLadderChannels; ++q)
+            if (q < x.channels) out[(size_t)q * x.n_temps_total] = stg[q];
+    }
+}
+
 __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
 {
     const int start = x.starts[l], R = x.sizes[l];
     const long long sweep = __ldcg(x.clock) + x.window_sweeps;
     const int parity = R > 2 ? (int)(__ldcg(x.clock + 1) & 1) : 0;
+    if (R <= 32 && x.channels <= kWarpLadderChannels) {
+        if (threadIdx.x < 32) exchange_ladder_warp(x, l, start, R, sweep, parity);
+        __syncthreads();
+        return;
+    }
     const int poff = start - l;
     const double *E = x.energies + start;
     float *B = x.betas + start;

@@ -42,6 +42,11 @@ CHANNELS = {
 }
 CHANNELS[MODEL_HE3_GAUSS] = CHANNELS[MODEL_HE3]
 CHANNELS[MODEL_KAWAMURA_GAUSS] = CHANNELS[MODEL_KAWAMURA]
+# Sweeps per window of a batch without replica exchange: nothing happens
+# between its windows but the clock tick, so long windows spare the strip
+# reload, write-back and launch of each short one.
+NO_EXCHANGE_WINDOW = 100
+
 # Models whose proposals have per-temperature widths sigma_t.
 GAUSSIAN_WIDTHS = (MODEL_XY, MODEL_KAWAMURA_GAUSS)
 
@@ -480,7 +485,7 @@ class LadderBatch:
                 n = min(left, to_ex)
                 out.append((n, n == to_ex))
             else:
-                n = min(left, 10)
+                n = min(left, NO_EXCHANGE_WINDOW)
                 out.append((n, False))
             s += n
             left -= n
@@ -493,7 +498,7 @@ class LadderBatch:
         partial windows at the ends launch directly.
         """
         plan = self._schedule(int(n_sweeps))
-        full = (self.exchange_interval, True) if self.pt else (10, False)
+        full = (self.exchange_interval, True) if self.pt else (NO_EXCHANGE_WINDOW, False)
         i = 0
         while i < len(plan):
             if graph and plan[i] == full:
