@@ -659,26 +659,6 @@ def run_workload(args, rank, world):
     return line
 
 
-def profile_resident(cluster_size=4, threads=512, steps=4):
-    """ncu driver for the bench's timed kernel: the XY ladder in production
-    mode (samples every 10 sweeps), `steps` resident launches of 100 sweeps
-    after one warm step."""
-    import torch
-
-    from mcgb.batch import LadderBatch
-    from mcgb.models.xy.model import XYModel
-
-    seed = 42 + L
-    b = LadderBatch(XYModel(J=1.0), [(L, temperatures())], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
-                    proposal="gaussian", sigma0=0.93, cluster_size=cluster_size, threads=threads,
-                    initial_states=[initial_angles(seed)])
-    b.allocate_samples(b.sweeps + SAMPLE_INTERVAL, SAMPLE_INTERVAL, (steps + 1) * SWEEPS_PER_STEP // SAMPLE_INTERVAL)
-    for _ in range(steps + 1):
-        b.run(SWEEPS_PER_STEP)
-    torch.cuda.synchronize()
-    print("profile resident done", b.resident)
-
-
 def profile_windows(cluster_size=4, threads=1024, workload="xy-pt-l128"):
     """Small fixed case for ncu: the workload's batch, 3 warm windows + 3 windows."""
     import ctypes
@@ -727,19 +707,14 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: set up the ladder, then launch 6 window kernels and exit")
     ap.add_argument("--profile-shape", default="4,1024", help="cluster_size,threads for --profile")
-    ap.add_argument("--profile-resident", action="store_true",
-                    help="profiling driver: the XY ladder's resident 100-sweep launches (production mode)")
     ap.add_argument("--workload", default="xy-pt-l128",
                     choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "kawamura-l96x64-reference-proposals",
                              "he3-ragged", "fss-ising", "fss-xy"],
                     help="configuration to time (default: the XY PT ladder the metric is quoted on)")
     args = ap.parse_args()
-    if args.profile or args.profile_resident:
+    if args.profile:
         c, t = (int(x) for x in args.profile_shape.split(","))
-        if args.profile_resident:
-            profile_resident(c, t)
-        else:
-            profile_windows(c, t, args.workload)
+        profile_windows(c, t, args.workload)
         return
     if args.warmup < 3:
         ap.error("warm-up must be at least 3 steps")
