@@ -188,6 +188,34 @@ int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s
     return cuda_status(err, name);
 }
 
+// The variant a batch runs: one or two plaquettes a thread with the streams
+// in registers when every strip fits (and the thread count is within that
+// variant's bound), else the global-memory streams variant (NPMAX = 0).
+template <class M>
+int pick_npmax(const mcgb_batch_window &w)
+{
+    long long npl = 0;
+    for (int r = 0; r < w.n_replicas; ++r) {
+        const int L = w.host_table[r].L;
+        const long long n = (long long)L * L / (4 * effective_cluster(L, w.cluster_size));
+        if (n > npl) npl = n;
+    }
+    if (npl <= w.threads && w.threads <= window_max_threads<M, 1>()) return 1;
+    if (npl <= 2LL * w.threads && w.threads <= window_max_threads<M, 2>()) return 2;
+    return 0;
+}
+
+template <class M>
+int launch_any(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s, const char *name)
+{
+    MCGB_REQUIRE(w.threads <= M::kMaxThreads, "%s: at most %d threads per CTA", name, M::kMaxThreads);
+    switch (pick_npmax<M>(w)) {
+    case 1: return launch_window<M, 1>(a, w, s, name);
+    case 2: return launch_window<M, 2>(a, w, s, name);
+    default: return launch_window<M, 0>(a, w, s, name);
+    }
+}
+
 template <class M, int NPMAX>
 int max_clusters_for(int C, int threads, size_t smem, int *out)
 {
@@ -212,6 +240,26 @@ int max_clusters_for(int C, int threads, size_t smem, int *out)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cuda_status(cudaOccupancyMaxActiveClusters(out, kern, &cfg), "cudaOccupancyMaxActiveClusters");
+}
+
+// Clusters resident at once for this shape, whichever variant the batch ends
+// up running (the smallest count over the variants the thread count allows).
+template <class M>
+int max_clusters_any(int C, int threads, size_t smem, int *out)
+{
+    MCGB_REQUIRE(threads <= M::kMaxThreads, "at most %d threads per CTA for this model", M::kMaxThreads);
+    int best = 0, n = 0;
+    if (int st = max_clusters_for<M, 0>(C, threads, smem, &best)) return st;
+    if (threads <= window_max_threads<M, 1>()) {
+        if (int st = max_clusters_for<M, 1>(C, threads, smem, &n)) return st;
+        if (n < best) best = n;
+    }
+    if (threads <= window_max_threads<M, 2>()) {
+        if (int st = max_clusters_for<M, 2>(C, threads, smem, &n)) return st;
+        if (n < best) best = n;
+    }
+    *out = best;
+    return MCGB_OK;
 }
 
 // Colour-major plane index of site (i, j) of a replica of size L.

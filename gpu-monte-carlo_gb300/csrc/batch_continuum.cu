@@ -628,18 +628,7 @@ __global__ void batch_energy64_continuum(int model, const void *state, const mcg
 template <class M>
 int continuum_launch(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s, const char *name)
 {
-    MCGB_REQUIRE(w.threads <= M::kMaxThreads, "%s: at most %d threads per CTA", name, M::kMaxThreads);
-    long long npl = 0;
-    for (int r = 0; r < w.n_replicas; ++r) {
-        const int L = w.host_table[r].L;
-        const long long n = (long long)L * L / (4 * effective_cluster(L, w.cluster_size));
-        if (n > npl) npl = n;
-    }
-    // One plaquette a thread, or two with the streams still in registers;
-    // beyond that (or above the two-plaquette variant's thread bound) the
-    // one-plaquette variant keeps the streams in global memory.
-    if (npl <= w.threads || w.threads > window_max_threads<M, 2>()) return launch_window<M, 1>(a, w, s, name);
-    return launch_window<M, 2>(a, w, s, name);
+    return launch_any<M>(a, w, s, name);
 }
 
 int continuum_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx)
@@ -668,9 +657,7 @@ int64_t continuum_smem(int model, int L, int C)
 template <class M>
 int continuum_clusters(int C, int threads, size_t smem, int *out)
 {
-    MCGB_REQUIRE(threads <= M::kMaxThreads, "at most %d threads per CTA for this model", M::kMaxThreads);
-    if (threads > window_max_threads<M, 2>()) return max_clusters_for<M, 1>(C, threads, smem, out);
-    return max_clusters_for<M, 2>(C, threads, smem, out);
+    return max_clusters_any<M>(C, threads, smem, out);
 }
 
 int continuum_max_clusters(int model, int C, int threads, size_t smem, int *out)

@@ -292,11 +292,8 @@ int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s, const 
     if (int st = validate_window(w)) return st;
     BatchArgs a = make_args(w);
     if (fx != nullptr) a.fx = *fx;
-    if (model == MCGB_MODEL_ISING)
-        return w.threads > 512 ? launch_window<IsingPolicy, 1>(a, w, s, "ising window")
-                               : launch_window<IsingPolicy, 2>(a, w, s, "ising window");
-    return w.threads > 512 ? launch_window<XYPolicy, 1>(a, w, s, "xy window")
-                           : launch_window<XYPolicy, 2>(a, w, s, "xy window");
+    if (model == MCGB_MODEL_ISING) return launch_any<IsingPolicy>(a, w, s, "ising window");
+    return launch_any<XYPolicy>(a, w, s, "xy window");
 }
 
 int64_t lattice_smem(int model, int L, int C)
@@ -306,11 +303,8 @@ int64_t lattice_smem(int model, int L, int C)
 
 int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out)
 {
-    if (model == MCGB_MODEL_ISING)
-        return threads > 512 ? max_clusters_for<IsingPolicy, 1>(C, threads, smem, out)
-                             : max_clusters_for<IsingPolicy, 2>(C, threads, smem, out);
-    return threads > 512 ? max_clusters_for<XYPolicy, 1>(C, threads, smem, out)
-                         : max_clusters_for<XYPolicy, 2>(C, threads, smem, out);
+    if (model == MCGB_MODEL_ISING) return max_clusters_any<IsingPolicy>(C, threads, smem, out);
+    return max_clusters_any<XYPolicy>(C, threads, smem, out);
 }
 
 int lattice_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s)

@@ -241,15 +241,25 @@ __device__ __forceinline__ void decide_pass(const typename M::Ctx &ctx, typename
 
 // Strips with more plaquettes than NK per thread keep their streams in
 // global memory and run propose + decide per plaquette, with full barriers.
+// A colour with the streams in global memory (strips with more plaquettes
+// than the register path holds).  Each thread walks its plaquettes with the
+// streams of the next two already requested, so the loads overlap with the
+// updates instead of each visit waiting on its own.
 template <class M, int C_>
 __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const typename M::Ctx &ctx,
                                                 typename M::Cell *cells, float *own, const StripCtx &g,
                                                 int64_t base, int64_t gplane, float &dacc, int &nacc)
 {
-    ulonglong2 *rng_g = static_cast<ulonglong2 *>(a.c.rng);
-    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
-        const int64_t idx = base + C_ * gplane + p;
-        ulonglong2 sv = rng_g[idx];
+    ulonglong2 *rng_g = static_cast<ulonglong2 *>(a.c.rng) + base + C_ * gplane;
+    const int T = blockDim.x;
+    const ulonglong2 zero = make_ulonglong2(0, 0);
+    int p = threadIdx.x;
+    ulonglong2 cur = p < g.NPL ? rng_g[p] : zero;
+    ulonglong2 nx1 = p + T < g.NPL ? rng_g[p + T] : zero;
+#pragma unroll 1
+    for (; p < g.NPL; p += T) {
+        const ulonglong2 nx2 = p + 2 * T < g.NPL ? rng_g[p + 2 * T] : zero;
+        ulonglong2 sv = cur;
         const Site s = make_site(p, g.LP);
         float *o = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
         typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
@@ -258,17 +268,19 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
         bool accepted;
         if constexpr (M::kPipeline) {
             const typename M::Prop pr = M::template propose<C_>(ctx, me, o, sv);
-            rng_g[idx] = sv;
+            rng_g[p] = sv;
             accepted = M::template decide<C_>(ctx, nb, me, o, pr, dE);
         } else {
             accepted = M::template update<C_>(ctx, nb, me, o, sv, dE);
-            rng_g[idx] = sv;
+            rng_g[p] = sv;
         }
         if (accepted) {
             dacc += dE;
             ++nacc;
             push_halo<C_>(cells, g, s, me);
         }
+        cur = nx1;
+        nx1 = nx2;
     }
 }
 
@@ -392,7 +404,9 @@ __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typena
 // replica `rep`: the CTA that completes the ladder's last replica runs the
 // ladder's exchange (the classic last-block pattern: every finisher fences
 // its energies and staged sample, then counts; no thread waits on another).
-__device__ __forceinline__ void ladder_finished(const FusedExchange &fx, const mcgb_replica &rep)
+// Out of line: in a resident launch the sweep state (streams, sites) stays
+// live across it, and inlined its registers pushed that state to the stack.
+static __device__ __noinline__ void ladder_finished(const FusedExchange &fx, const mcgb_replica &rep)
 {
     __shared__ int last;
     if (threadIdx.x == 0) {
@@ -530,7 +544,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                     *static_cast<Cell *>(__cluster_map_shared_rank(cells + c * g.PS + s.pc, g.dn)) = me;
             }
 
-        const bool regs = NPMAX > 0 && g.NPL <= NPMAX * T;
+        // NPMAX > 0: the streams live in registers (the host launches this
+        // variant only when every strip fits); NPMAX = 0: global memory.
+        constexpr bool regs = NPMAX > 0;
         ulonglong2 st[NK][4];
         Site sites[NK];
 #pragma unroll
@@ -570,8 +586,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             // This sweep's accepted energy changes (at most a few terms per
             // thread), folded into the compensated running sum once per sweep.
             float dacc = 0.0f;
-            if (!M::kPipeline && regs) {
-                if constexpr (!M::kPipeline) {
+            if constexpr (!M::kPipeline && regs) {
+                {
                     cluster_wait();
                     MCGB_COMBINE_PENDING()
                     fused_pass<M, NK, 0>(ctx, cells, own, g, sites, st, dacc, nacc);
@@ -588,8 +604,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                     fused_pass<M, NK, 3>(ctx, cells, own, g, sites, st, dacc, nacc);
                     cluster_arrive();
                 }
-            } else if (regs) {
-                if constexpr (M::kPipeline) {
+            } else if constexpr (regs) {
+                {
                 // Invariant: this thread has arrived at the barrier that
                 // follows the previous phase and not yet waited.
                 propose_pass<M, NK, 0>(ctx, cells, own, g, sites, st, pa);
@@ -613,6 +629,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 cluster_arrive();
                 }
             } else {
+                (void)sites;
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
                 global_rng_pass<M, 0>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
