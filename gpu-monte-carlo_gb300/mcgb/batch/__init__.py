@@ -207,8 +207,27 @@ class LadderBatch:
         # ---------------------------------------------------------- device buffers
         site = int(np.prod(self.site_shape, dtype=np.int64))
         self.elem_bytes = self.dtype.itemsize * site
-        self.state = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
-        self.rng = DeviceArray((self.n_sites,), XOROSHIRO128P_DTYPE)
+        # The chain state -- spins/angles, RNG streams, running energies and,
+        # for XY and Kawamura, the (cos, sin) cache -- lives in one device
+        # allocation (256-byte aligned pieces), so a host round trip is one
+        # copy each way.
+        has_aux = self.model_id in (MODEL_XY, MODEL_KAWAMURA, MODEL_KAWAMURA_GAUSS)
+        pieces = [("state", (self.n_sites,) + self.site_shape, self.dtype),
+                  ("rng", (self.n_sites,), XOROSHIRO128P_DTYPE),
+                  ("e_run", (2 * self.R,), np.dtype(np.float32))]
+        if has_aux:
+            pieces.append(("aux", (self.n_sites, 2), np.dtype(np.float32)))
+        offsets, total = [], 0
+        for _, shape, dt in pieces:
+            offsets.append(total)
+            total += -(-int(np.prod(shape, dtype=np.int64)) * np.dtype(dt).itemsize // 256) * 256
+        import torch as _t
+        self._chain = _t.zeros(max(total, 1), dtype=_t.uint8, device=_t.device("cuda", _t.cuda.current_device()))
+        for (name, shape, dt), off in zip(pieces, offsets):
+            nb = int(np.prod(shape, dtype=np.int64)) * np.dtype(dt).itemsize
+            setattr(self, name, DeviceArray(shape, dt, _storage=self._chain[off:off + max(nb, 1)]))
+        if not has_aux:
+            self.aux = None
         ref_state = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
         ref_rng = DeviceArray((self.n_sites,), XOROSHIRO128P_DTYPE)
         for k, (L, T) in enumerate(self.ladders):
@@ -230,7 +249,6 @@ class LadderBatch:
         local = np.concatenate([np.arange(n, dtype=np.int32) for n in sizes])
         self.w2t = to_device(local)
         self.t2w = to_device(local)
-        self.e_run = device_zeros(2 * self.R, np.float32)
         self.energies = device_zeros(self.R, np.float64)
         self.accepted = device_zeros(self.R, np.int64)
         self.accepted_prev = device_zeros(self.R, np.int64)
@@ -239,8 +257,6 @@ class LadderBatch:
         self.drift = device_zeros(self.R, np.float64)
         self.sigma_t = to_device(np.full(self.R, sigma0, np.float32))
         self.staging = device_zeros((len(self.channels), self.R), np.float64)
-        self.aux = (DeviceArray((self.n_sites, 2), np.float32)
-                    if self.model_id in (MODEL_XY, MODEL_KAWAMURA, MODEL_KAWAMURA_GAUSS) else None)
         self.sweeps = 0
         self.exchange_rounds = 0
 
@@ -582,36 +598,30 @@ class LadderBatch:
         self.exchange_rounds += 1
 
     # ------------------------------------------------------------ host I/O
-    def _host_fields(self):
-        fields = {"state": self.state, "rng": self.rng, "e_run": self.e_run}
-        if self.aux is not None:
-            fields["aux"] = self.aux
-        return fields
-
     def pinned_state_buffers(self):
-        """Pinned host byte buffers for the chain state in the engine layout:
-        spins/angles, RNG streams, the running energies and, for XY and
-        Kawamura, the (cos, sin) cache."""
+        """A pinned host buffer for the whole chain state (spins/angles, RNG
+        streams, running energies, the (cos, sin) cache), engine layout."""
         import torch as _t
-        return {k: _t.empty(v.nbytes, dtype=_t.uint8, pin_memory=True) for k, v in self._host_fields().items()}
+        return {"chain": _t.empty(self._chain.numel(), dtype=_t.uint8, pin_memory=True)}
 
     def upload_state(self, host, recompute=False):
-        """Asynchronous host-to-device copy from pinned buffers.  A buffer set
-        from download_state resumes the chain exactly; when it holds only
-        ``state`` and ``rng`` (or ``recompute`` is set), the (cos, sin) cache
-        and the exact energies are rebuilt on the device instead."""
-        for k, arr in self._host_fields().items():
-            if k in host:
-                arr.raw().copy_(host[k], non_blocking=True)
-        if recompute or "e_run" not in host or (self.aux is not None and "aux" not in host):
+        """Asynchronous host-to-device copy from pinned buffers.  A buffer from
+        pinned_state_buffers/download_state resumes the chain exactly (one
+        copy); a dict of ``state`` and ``rng`` bytes alone (engine layout)
+        uploads those, then rebuilds the (cos, sin) cache and the exact
+        energies on the device, as does ``recompute``."""
+        if "chain" in host:
+            self._chain.copy_(host["chain"], non_blocking=True)
+        else:
+            self.state.raw().copy_(host["state"], non_blocking=True)
+            self.rng.raw().copy_(host["rng"], non_blocking=True)
+        if recompute or "chain" not in host:
             self.refresh_aux()
             self.recompute_energy()
 
     def download_state(self, host):
-        """Asynchronous device-to-host copy of the chain state into pinned buffers."""
-        for k, arr in self._host_fields().items():
-            if k in host:
-                host[k].copy_(arr.raw(), non_blocking=True)
+        """Asynchronous device-to-host copy of the chain state (one copy)."""
+        host["chain"].copy_(self._chain, non_blocking=True)
 
     def checkpoint(self):
         """Everything needed to resume the chain bit-exactly, as host arrays."""
