@@ -238,6 +238,7 @@ struct FusedExchange {
     int32_t *error;        // [1] set when a wait for the epoch gave up
     int enabled;
     int n_windows;         // > 1: a resident launch (one replica per cluster, cooperative)
+    long long wait_limit;  // polls of the epoch before a wait gives up
 };
 
 }  // namespace mcgb

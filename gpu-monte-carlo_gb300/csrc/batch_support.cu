@@ -173,8 +173,18 @@ extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w,
     fx.error = nullptr;
     fx.enabled = 1;
     fx.n_windows = 1;
+    fx.wait_limit = kEpochSpinLimit;
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
+}
+
+static long long g_wait_limit = kEpochSpinLimit;
+
+extern "C" int64_t mcgb_batch_set_wait_limit(int64_t polls)
+{
+    const long long old = g_wait_limit;
+    g_wait_limit = polls < 0 ? kEpochSpinLimit : polls;
+    return old;
 }
 
 extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
@@ -198,6 +208,7 @@ extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, co
     fx.error = sync + pt->n_ladders + 2;
     fx.enabled = 1;
     fx.n_windows = n_windows;
+    fx.wait_limit = g_wait_limit;
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
 }

@@ -445,7 +445,7 @@ __device__ __forceinline__ int load_acquire(const int32_t *p)
     return v;
 }
 
-// Iterations of the epoch wait (each sleeps 32..256 ns) before a resident
+// Default polls of the epoch wait (each sleeps 32..256 ns) before a resident
 // launch gives up: ~1 s, far beyond a window's length.
 constexpr long long kEpochSpinLimit = 1ll << 22;
 
@@ -470,7 +470,7 @@ __device__ __forceinline__ void window_finished(const FusedExchange &fx, const W
     }
     unsigned ns = 32;
     for (long long it = 0; load_acquire(fx.epoch) < win + 1; ++it) {
-        if (it >= kEpochSpinLimit) {
+        if (it >= fx.wait_limit) {
             atomicExch(fx.error, 1);
             break;
         }

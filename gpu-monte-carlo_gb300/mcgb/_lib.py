@@ -56,6 +56,7 @@ SIGNATURES = {
     "mcgb_batch_exchange": [_P, _P, _P],
     "mcgb_batch_window_exchange": [_I, _P, _P, _P, _P],
     "mcgb_batch_run_resident": [_I, _P, _P, _P, _I, _P],
+    "mcgb_batch_set_wait_limit": [ctypes.c_int64],
     "mcgb_batch_clock_tick": [_P, _I, _I, _P],
     "mcgb_batch_tune_sigma": [_P, _P, _P, _P, _P, _I, _I, _F, _F, _F, _F, _P],
     "mcgb_batch_window_exchange_noalloc": [_I, _P, _P, _P],
@@ -66,6 +67,7 @@ RESTYPES = {
     "mcgb_last_error": ctypes.c_char_p,
     "mcgb_version": ctypes.c_char_p,
     "mcgb_batch_smem_bytes": ctypes.c_int64,
+    "mcgb_batch_set_wait_limit": ctypes.c_int64,
 }
 
 EINVAL, ECUDA, ENOMEM, ETIMEOUT = -1, -2, -3, -4

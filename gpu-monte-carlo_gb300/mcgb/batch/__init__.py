@@ -577,6 +577,14 @@ class LadderBatch:
         g.replay()
         self._advance(step[0], step[1], count)
 
+    def set_wait_limit(self, polls):
+        """Polls a resident launch's wait between windows makes before giving
+        up (None: the default, about a second); returns the previous value.
+        Captured graphs hold the old limit, so they are dropped."""
+        self._graphs.clear()
+        self._resident_checked = False
+        return int(_lib.load().mcgb_batch_set_wait_limit(-1 if polls is None else int(polls)))
+
     def check_errors(self):
         """Raise MCGBTimeout if a resident launch gave up waiting between
         windows (its results are then unreliable); clears the flag."""

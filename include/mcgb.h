@@ -319,6 +319,12 @@ int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb
  * n_windows = 1 is mcgb_batch_window_exchange. */
 int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                             int32_t *sync, int n_windows, void *stream);
+/* No counterpart in the reference.  Polls of a resident launch's wait
+ * between windows before it gives up and raises the error flag (default
+ * 2^22, about a second; negative restores the default).  Applies to later
+ * calls; returns the previous value.  A small limit makes the waits run out,
+ * which is how the timeout path is tested. */
+int64_t mcgb_batch_set_wait_limit(int64_t polls);
 /* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
  * a captured graph of windows and exchanges can be replayed. */
 int mcgb_batch_clock_tick(int64_t *clock, int n_sweeps, int exchanged, void *stream);

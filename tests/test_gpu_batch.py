@@ -396,3 +396,29 @@ def test_host_round_trip_resumes_the_chain_exactly():
     b.upload_state({"state": state_bytes, "rng": rng_bytes})
     drift = b.recompute_energy().copy_to_host()
     assert np.all(np.abs(drift) < 1e-6 * L * L)
+
+
+def test_resident_wait_that_runs_out_is_reported_and_the_batch_recovers():
+    """Failure detection: with a wait limit of zero polls the clusters of a
+    resident launch give up waiting for the window epoch at once; the kernel
+    raises its error flag and returns (no hang), check_errors() reports it as
+    MCGBTimeout and clears the counters, and later launches run normally."""
+    from mcgb import _lib
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+    b = LadderBatch(XYModel(), [(16, np.geomspace(0.8, 1.2, 4))], exchange_interval=2, proposal="gaussian",
+                    cluster_size=2, threads=128)
+    assert b.resident
+    b.run(20)
+    b.check_errors()
+    old = b.set_wait_limit(0)
+    try:
+        b.run(20)
+        with pytest.raises(_lib.MCGBTimeout):
+            b.check_errors()
+    finally:
+        b.set_wait_limit(None)
+    assert old == b.set_wait_limit(None)
+    b.run(20)
+    b.check_errors()
+    assert b.sync.copy_to_host().tolist() == [0] * (len(b.ladders) + 3)
