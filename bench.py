@@ -254,7 +254,8 @@ def run_mcgb(args, rank, world):
     temps = temperatures()
     seed = ladder_seed(rank)
     batch = LadderBatch(XYModel(J=1.0), [(L, temps)], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
-                        proposal="gaussian", sigma0=1.0, initial_states=[initial_angles(seed)])
+                        proposal="gaussian", sigma0=1.0, initial_states=[initial_angles(seed)],
+                        resident=not args.no_resident)
     batch.autotune()
     # Warm-up: thermalise and tune the proposal widths (adaptation stops here).
     batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=True)
@@ -707,6 +708,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: set up the ladder, then launch 6 window kernels and exit")
     ap.add_argument("--profile-shape", default="4,1024", help="cluster_size,threads for --profile")
+    ap.add_argument("--no-resident", action="store_true",
+                    help="one launch per window instead of resident multi-window launches (for profiling)")
     ap.add_argument("--workload", default="xy-pt-l128",
                     choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "kawamura-l96x64-reference-proposals",
                              "he3-ragged", "fss-ising", "fss-xy"],

@@ -188,9 +188,10 @@ int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s
     return cuda_status(err, name);
 }
 
-// The variant a batch runs: one or two plaquettes a thread with the streams
-// in registers when every strip fits (and the thread count is within that
-// variant's bound), else the global-memory streams variant (NPMAX = 0).
+// The variant a batch runs: the streams in registers when every strip fits,
+// preferring the two-plaquette variant (compiled for fewer threads, so with
+// the larger register budget) whenever the thread count allows it; else the
+// global-memory streams variant (NPMAX = 0).
 template <class M>
 int pick_npmax(const mcgb_batch_window &w)
 {
@@ -200,8 +201,8 @@ int pick_npmax(const mcgb_batch_window &w)
         const long long n = (long long)L * L / (4 * effective_cluster(L, w.cluster_size));
         if (n > npl) npl = n;
     }
-    if (npl <= w.threads && w.threads <= window_max_threads<M, 1>()) return 1;
     if (npl <= 2LL * w.threads && w.threads <= window_max_threads<M, 2>()) return 2;
+    if (npl <= w.threads && w.threads <= window_max_threads<M, 1>()) return 1;
     return 0;
 }
 
