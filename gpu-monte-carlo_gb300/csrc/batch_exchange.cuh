@@ -226,19 +226,44 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
     __syncthreads();
 }
 
-// Completion bookkeeping of the fused window + exchange launch.  `sync` holds
-// one counter per ladder, one for the launch, the resident launch's window
-// epoch and its error flag; the counters and the epoch are zero between
-// launches.
+// Bookkeeping of the fused window + exchange launch, carved out of one int32
+// array `sync` of 6 * n_replicas + 2 entries (16-byte aligned, zero before
+// the first launch; the pair counts run on from launch to launch):
+//   post     [n_replicas] x 16 B  per global temperature slot: the energy
+//                                 (double), then beta (float bits, low word)
+//                                 and the local walker id (high word) of the
+//                                 walker that last finished at that slot
+//   arrive   [n_replicas]         per pair, at its left slot: walkers counted
+//   decided  [n_replicas]         per pair: (round + 1) << 1 | swapped
+//   launch_done [1], error [1]
 struct FusedExchange {
     ExchangeArgs ex;
-    int32_t *ladder_done;  // [n_ladders]
-    int32_t *launch_done;  // [1]
-    int32_t *epoch;        // [1] resident launches: windows completed so far
-    int32_t *error;        // [1] set when a wait for the epoch gave up
+    double2 *post;
+    unsigned *arrive;
+    int32_t *decided;
+    int32_t *launch_done;
+    int32_t *error;        // set when a wait for a pair's decision gave up
     int enabled;
     int n_windows;         // > 1: a resident launch (one replica per cluster, cooperative)
-    long long wait_limit;  // polls of the epoch before a wait gives up
+    long long wait_limit;  // polls of a pair's decision before a wait gives up
 };
+
+__host__ __device__ inline long long fused_sync_words(int n_replicas) { return 6ll * n_replicas + 2; }
+
+inline FusedExchange make_fused(const ExchangeArgs &ex, int32_t *sync, int n_windows, long long wait_limit)
+{
+    const int n = ex.n_replicas;
+    FusedExchange fx;
+    fx.ex = ex;
+    fx.post = reinterpret_cast<double2 *>(sync);
+    fx.arrive = reinterpret_cast<unsigned *>(sync + 4ll * n);
+    fx.decided = sync + 5ll * n;
+    fx.launch_done = sync + 6ll * n;
+    fx.error = sync + 6ll * n + 1;
+    fx.enabled = 1;
+    fx.n_windows = n_windows;
+    fx.wait_limit = wait_limit;
+    return fx;
+}
 
 }  // namespace mcgb

@@ -165,25 +165,18 @@ extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w,
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
     if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
-    FusedExchange fx;
-    fx.ex = make_exchange_args(*w, *pt);
-    fx.ladder_done = sync;
-    fx.launch_done = sync + pt->n_ladders;
-    fx.epoch = nullptr;
-    fx.error = nullptr;
-    fx.enabled = 1;
-    fx.n_windows = 1;
-    fx.wait_limit = kEpochSpinLimit;
+    MCGB_REQUIRE((reinterpret_cast<uintptr_t>(sync) & 15) == 0, "window_exchange: sync must be 16-byte aligned");
+    const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, 1, kWaitSpinLimit);
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
 }
 
-static long long g_wait_limit = kEpochSpinLimit;
+static long long g_wait_limit = kWaitSpinLimit;
 
 extern "C" int64_t mcgb_batch_set_wait_limit(int64_t polls)
 {
     const long long old = g_wait_limit;
-    g_wait_limit = polls < 0 ? kEpochSpinLimit : polls;
+    g_wait_limit = polls < 0 ? kWaitSpinLimit : polls;
     return old;
 }
 
@@ -200,15 +193,8 @@ extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, co
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
     if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
-    FusedExchange fx;
-    fx.ex = make_exchange_args(*w, *pt);
-    fx.ladder_done = sync;
-    fx.launch_done = sync + pt->n_ladders;
-    fx.epoch = sync + pt->n_ladders + 1;
-    fx.error = sync + pt->n_ladders + 2;
-    fx.enabled = 1;
-    fx.n_windows = n_windows;
-    fx.wait_limit = g_wait_limit;
+    MCGB_REQUIRE((reinterpret_cast<uintptr_t>(sync) & 15) == 0, "run_resident: sync must be 16-byte aligned");
+    const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, n_windows, g_wait_limit);
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
 }

@@ -400,40 +400,18 @@ __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typena
     }
 }
 
-// Fused exchange, run by the rank-0 CTA of a cluster after it finished
-// replica `rep`: the CTA that completes the ladder's last replica runs the
-// ladder's exchange (the classic last-block pattern: every finisher fences
-// its energies and staged sample, then counts; no thread waits on another).
-// Out of line: in a resident launch the sweep state (streams, sites) stays
-// live across it, and inlined its registers pushed that state to the stack.
-static __device__ __noinline__ void ladder_finished(const FusedExchange &fx, const mcgb_replica &rep)
-{
-    __shared__ int last;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(fx.ladder_done + rep.ladder, 1) == rep.n_temps - 1;
-        if (last) {
-            fx.ladder_done[rep.ladder] = 0;  // every replica of the ladder has counted
-            __threadfence();
-        }
-    }
-    __syncthreads();
-    if (last) exchange_ladder(fx.ex, rep.ladder);
-}
-
 // After a cluster's whole work list (thread 0 of its rank-0 CTA): the last
-// cluster to finish advances the device clock, after every ladder's exchange
-// has read it, and resets the launch counter (and a resident launch's epoch).
+// cluster to finish advances the device clock by the launch's windows (every
+// cluster has read it at its start) and resets the launch counter.
 __device__ __forceinline__ void launch_finished(const FusedExchange &fx, const WindowCommon &cm, int n_clusters)
 {
     __threadfence();
     if (atomicAdd(fx.launch_done, 1) == n_clusters - 1) {
         __threadfence();
         long long *clock = const_cast<long long *>(cm.clock);
-        clock[0] = __ldcg(clock) + cm.n_sweeps;
-        clock[1] = __ldcg(clock + 1) + 1;
+        clock[0] = __ldcg(clock) + (long long)cm.n_sweeps * fx.n_windows;
+        clock[1] = __ldcg(clock + 1) + fx.n_windows;
         *fx.launch_done = 0;
-        if (fx.n_windows > 1) *fx.epoch = 0;
         __threadfence();
     }
 }
@@ -445,37 +423,156 @@ __device__ __forceinline__ int load_acquire(const int32_t *p)
     return v;
 }
 
-// Default polls of the epoch wait (each sleeps 32..256 ns) before a resident
-// launch gives up: ~1 s, far beyond a window's length.
-constexpr long long kEpochSpinLimit = 1ll << 22;
+// Default polls of a pair's decision (each sleeps 32..256 ns) before a wait
+// between the windows of a resident launch gives up: ~1 s, far beyond a
+// window's length.
+constexpr long long kWaitSpinLimit = 1ll << 22;
 
-// Between two windows of a resident launch (thread 0 of each cluster's rank-0
-// CTA, after its ladder bookkeeping): count the cluster; the last one
-// advances the clock, resets the count and publishes window `win` as done;
-// every cluster then waits for that epoch.  All clusters are co-resident (a
-// cooperative launch), so the wait ends; it is bounded all the same: on
-// giving up it raises the error flag and goes on (the host reports it).
-__device__ __forceinline__ void window_finished(const FusedExchange &fx, const WindowCommon &cm, int n_clusters,
-                                                int win)
+// The fused replica exchange of walker r after window `win` of a launch of
+// n_windows: core/parallel_tempering.py:35-91, decided pair by pair as soon
+// as both walkers of a pair are done, so no walker waits for the rest of its
+// ladder.  Lane 0 of the walker's rank-0 warp 0 posts (energy, beta, id) at
+// the walker's slot and counts it at its pair; the second to arrive decides
+// with the pair's stream and writes the swap counters, maps and betas of
+// both.  Between the windows of a resident launch the first to arrive waits
+// for that decision, bounded: on giving up it raises the error flag and
+// keeps its slot (the host then reports the launch as failed).  After the
+// last window nobody waits: the decider settles both walkers.  Every round
+// brings exactly two arrivals to each of its pairs, and a walker reaches a
+// pair's next round only after that pair's decision, so the arrival count
+// names the round and a decision word cannot be mistaken for an earlier one.
+// Settling a walker at its new slot -- round-trip counters and the staged
+// window-end sample -- is spread over the warp.  Decisions, maps, counters,
+// round trips and sample slots are exchange_ladder's on the same window.
+// Called by the 32 threads of warp 0; kept light in registers, because the
+// window kernel keeps its sweep state live across the call.
+static __device__ __noinline__ void pair_finished(const FusedExchange &fx, const mcgb_replica &rep, int r, int win,
+                                                  int n_windows)
 {
-    __threadfence();
-    if (atomicAdd(fx.launch_done, 1) == n_clusters - 1) {
-        __threadfence();
-        long long *clock = const_cast<long long *>(cm.clock);
-        clock[0] = __ldcg(clock) + cm.n_sweeps;
-        clock[1] = __ldcg(clock + 1) + 1;
-        *fx.launch_done = 0;
-        __threadfence();
-        atomicExch(fx.epoch, win + 1);
-    }
-    unsigned ns = 32;
-    for (long long it = 0; load_acquire(fx.epoch) < win + 1; ++it) {
-        if (it >= fx.wait_limit) {
-            atomicExch(fx.error, 1);
-            break;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const ExchangeArgs &x = fx.ex;
+    const int start = rep.ladder_start, R = rep.n_temps, w = r - start;
+    const long long sweep = __ldcg(x.clock) + (long long)(win + 1) * x.window_sweeps;
+    const bool wait = win + 1 < n_windows;
+    // walker w ends at slot t0 (-1: unknown); walker w1 (-1: none) at t1
+    int t0 = -1, w1 = -1, t1 = -1;
+    if (lane == 0) {
+        const int parity = R > 2 ? (int)((__ldcg(x.clock + 1) + win) & 1) : 0;
+        const int s = __ldcg(x.w2t + r);
+        int left = -1;
+        if (R >= 2) {
+            if (s >= parity && ((s - parity) & 1) == 0 && s < R - 1)
+                left = s;
+            else if (s >= 1 + parity && ((s - 1 - parity) & 1) == 0)
+                left = s - 1;
         }
-        __nanosleep(ns);
-        if (ns < 256) ns <<= 1;
+        if (left < 0) {
+            t0 = s;  // no partner this round
+        } else {
+            const int partner = s == left ? left + 1 : left;
+            const double e = __ldcg(x.energies + r);
+            const float b = __ldcg(x.betas + r);
+            const unsigned long long tag = ((unsigned long long)(unsigned)w << 32) | __float_as_uint(b);
+            fx.post[start + s] = make_double2(e, __longlong_as_double((long long)tag));
+            __threadfence();
+            const unsigned old = atomicAdd(fx.arrive + start + left, 1u);
+            const int round = (int)(((old >> 1) + 1u) & 0x3fffffffu);
+            if (old & 1u) {
+                __threadfence();
+                const int poff = start - rep.ladder, np = x.n_pairs_total;
+                const double2 q = __ldcg(fx.post + start + partner);
+                long long *cnt = x.counts + poff + left;
+                long long att = __ldcg(cnt), acc = __ldcg(cnt + np), nonf = __ldcg(cnt + 2 * np);
+                ulonglong2 st = __ldcg(x.rng + poff + left);
+                const unsigned long long qtag = (unsigned long long)__double_as_longlong(q.y);
+                const int wq = (int)(qtag >> 32);
+                const float bq = __uint_as_float((unsigned)qtag);
+                const bool me_left = s == left;
+                const double ea = me_left ? e : q.x, eb = me_left ? q.x : e;
+                const float ba = me_left ? b : bq, bb = me_left ? bq : b;
+                int swapped = 0;
+                att += 1;
+                if (!isfinite(ea) || !isfinite(eb)) {
+                    nonf += 1;
+                } else {
+                    const double log_ratio = ((double)ba - (double)bb) * (ea - eb);
+                    const double u = xoro_uniform_f64(st);
+                    x.rng[poff + left] = st;
+                    if (log_ratio >= 0.0 || u == 0.0 || log(u) < log_ratio) {
+                        swapped = 1;
+                        acc += 1;
+                    }
+                }
+                cnt[0] = att;
+                cnt[np] = acc;
+                cnt[2 * np] = nonf;
+                if (swapped) {
+                    const int wa = me_left ? w : wq, wb = me_left ? wq : w;
+                    x.t2w[start + left] = wb;
+                    x.t2w[start + left + 1] = wa;
+                    x.w2t[start + wa] = left + 1;
+                    x.w2t[start + wb] = left;
+                    x.betas[start + wa] = bb;
+                    x.betas[start + wb] = ba;
+                }
+                __threadfence();
+                atomicExch(fx.decided + start + left, round << 1 | swapped);
+                t0 = swapped ? partner : s;
+                if (!wait) {
+                    w1 = wq;
+                    t1 = swapped ? s : partner;
+                }
+            } else if (wait) {
+                unsigned ns = 32;
+                for (long long it = 0;; ++it) {
+                    if (it >= fx.wait_limit) {
+                        atomicExch(fx.error, 1);
+                        break;
+                    }
+                    const int v = load_acquire(fx.decided + start + left);
+                    if ((v >> 1) == round) {
+                        t0 = (v & 1) ? partner : s;
+                        break;
+                    }
+                    __nanosleep(ns);
+                    if (ns < 256) ns <<= 1;
+                }
+            }
+        }
+    }
+    t0 = __shfl_sync(full, t0, 0);
+    w1 = __shfl_sync(full, w1, 0);
+    t1 = __shfl_sync(full, t1, 0);
+    __syncwarp();  // orders lane 0's acquire before the other lanes' reads
+    // Settle: lane k < 2 keeps walker k's round-trip counters, then the lanes
+    // copy the staged sample channels to the walkers' new slots.
+    const int wk = lane == 0 ? w : w1, tk = lane == 0 ? t0 : t1;
+    const int n = x.n_replicas;
+    if (lane < 2 && tk >= 0 && (tk == 0 || tk == R - 1)) {
+        long long *tr = x.trips + start + wk;
+        const long long origin = __ldcg(tr), visited = __ldcg(tr + n), sweep0 = __ldcg(tr + 2 * n),
+                        ntrips = __ldcg(tr + 3 * n), tsweeps = __ldcg(tr + 4 * n);
+        if (origin < 0) {
+            tr[0] = tk;
+            tr[2 * n] = sweep;
+        } else if (tk != origin) {
+            tr[n] = 1;
+        } else if (visited) {
+            tr[3 * n] = ntrips + 1;
+            tr[4 * n] = tsweeps + (sweep - sweep0);
+            tr[2 * n] = sweep;
+            tr[n] = 0;
+        }
+    }
+    if (x.staging == nullptr || x.samples == nullptr) return;
+    const int slot = sample_slot(sweep, x.first_sample_sweep, x.sample_interval, x.n_slots);
+    if (slot < 0) return;
+    double *out = x.samples + (size_t)slot * x.channels * x.n_temps_total + start;
+    for (int j = lane; j < 2 * x.channels; j += 32) {
+        const int k = j < x.channels ? 0 : 1, q = j - k * x.channels;
+        const int wj = k ? w1 : w, tj = k ? t1 : t0;
+        if (tj >= 0) out[(size_t)q * x.n_temps_total + tj] = __ldcg(x.staging + (size_t)q * n + start + wj);
     }
 }
 
@@ -560,13 +657,16 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
         }
         // A resident launch runs n_windows windows with the strip on chip,
-        // exchanging (and waiting for every cluster) between them; values the
-        // exchange rewrites are re-read past L1 at each window start.
+        // exchanging between them (each walker waits for its pair's decision
+        // only); values the exchange rewrites are re-read past L1 at each
+        // window start.
         const int n_windows = a.fx.enabled && a.fx.n_windows > 1 ? a.fx.n_windows : 1;
         for (int win = 0; win < n_windows; ++win) {
         const typename M::Ctx ctx = M::prepare(a, r, rep);
         const float e_hi0 = __ldcg(cm.e_run + 2 * r), e_lo0 = __ldcg(cm.e_run + 2 * r + 1);
-        const long long sweep0 = __ldcg(cm.clock);
+        // A fused launch advances the clock once, at its end, after every
+        // cluster has finished its windows: within it the clock stands still.
+        const long long sweep0 = __ldcg(cm.clock) + (long long)win * cm.n_sweeps;
         const int tslot = rep.ladder_start + __ldcg(cm.w2t + r);
         cluster_arrive();
 
@@ -699,6 +799,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         }
         cluster.sync();
         if (rank == 0 && tid == 0) {
+            double e_now;
             FSum de, na, ex;
             for (int k = 0; k < C; ++k) {
                 const float2 *pk = parts + k * NP + NS;
@@ -711,26 +812,24 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 const double e = M::finish_energy(ctx, ex.value());
                 hi = (float)e;
                 lo2 = (float)(e - (double)hi);
-                cm.energies[r] = e;
+                e_now = e;
             } else {
                 // Compensated (hi, lo) float update of the running energy.
                 float s1, e1;
                 two_sum(e_hi0, de.hi, s1, e1);
                 const float lo = e_lo0 + e1 + de.lo;
                 two_sum(s1, lo, hi, lo2);
-                cm.energies[r] = (double)hi + (double)lo2;
+                e_now = (double)hi + (double)lo2;
             }
+            cm.energies[r] = e_now;
             cm.e_run[2 * r] = hi;
             cm.e_run[2 * r + 1] = lo2;
             cm.accepted[r] = __ldcg(cm.accepted + r) + (long long)na.value();
         }
+        __syncwarp();
+        if (a.fx.enabled && rank == 0 && tid < 32) pair_finished(a.fx, rep, r, win, n_windows);
+        __syncwarp();  // the aligned cluster barrier needs warp 0 converged again
         cluster.sync();
-        if (a.fx.enabled && rank == 0) ladder_finished(a.fx, rep);
-        if (win + 1 < n_windows) {
-            if (rank == 0 && tid == 0) window_finished(a.fx, cm, (int)(gridDim.x / C), win);
-            __syncwarp();  // the aligned cluster barrier needs warp 0 converged again
-            cluster.sync();
-        }
         }  // windows
     }
     if (a.fx.enabled && rank == 0 && tid == 0) launch_finished(a.fx, cm, (int)(gridDim.x / C));

@@ -269,9 +269,10 @@ class LadderBatch:
                 pair_rng[po:po + n - 1].raw().copy_(sub.raw())
             self.pair_rng = pair_rng
             self.swap_counts = device_zeros((3, n_pairs), np.int64)
-            # Completion counters of the fused window + exchange launch, then
-            # the resident launch's window epoch and its error flag.
-            self.sync = device_zeros(n_l + 3, np.int32)
+            # Bookkeeping of the fused window + exchange launch: per-slot
+            # posts (4 words each), per-pair arrival counts and decisions,
+            # the launch counter, then the error flag.
+            self.sync = device_zeros(6 * self.R + 2, np.int32)
             trips = np.zeros((5, self.R), np.int64)
             trips[0] = -1
             trips[2] = -1
@@ -587,13 +588,30 @@ class LadderBatch:
 
     def check_errors(self):
         """Raise MCGBTimeout if a resident launch gave up waiting between
-        windows (its results are then unreliable); clears the flag."""
+        windows.  Its samples and exchange statistics are then unreliable and
+        its slot maps may disagree; before raising, the maps are rebuilt from
+        w2t (identity for a ladder whose w2t is no permutation), the betas
+        set to match and the sync array zeroed, so later runs are sound."""
         if not self.pt:
             return
         flag = self.sync.copy_to_host()[-1]
         if flag:
-            self.sync.copy_to_device(np.zeros(len(self.ladders) + 3, np.int32))
+            self._repair_maps()
+            self.sync.copy_to_device(np.zeros(len(self.sync), np.int32))
             raise _lib.MCGBTimeout(-4, "a resident launch timed out waiting between windows")
+
+    def _repair_maps(self):
+        w2t = self.w2t.copy_to_host()
+        t2w = np.empty_like(w2t)
+        for s0, n in zip(self.ladder_starts_host, self.ladder_sizes_host):
+            local = w2t[s0:s0 + n]
+            if not np.array_equal(np.sort(local), np.arange(n)):
+                local[:] = np.arange(n)
+            t2w[s0:s0 + n] = np.argsort(local)
+        self.w2t.copy_to_device(w2t)
+        self.t2w.copy_to_device(t2w.astype(np.int32))
+        starts = np.repeat(self.ladder_starts_host, self.ladder_sizes_host)
+        self.betas.copy_to_device(self._initial_betas[starts + w2t])
 
     def exchange_now(self):
         """Attempt one matching now (fresh energies from the running cache)."""

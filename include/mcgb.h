@@ -299,11 +299,14 @@ int mcgb_batch_window_exchange_noalloc(int model, const mcgb_batch_window *w, co
 /* No counterpart in the reference (it launches four colour kernels per sweep
  * and one exchange kernel per round, core/parallel_tempering.py:245-269).
  * mcgb_batch_window_run, mcgb_batch_exchange and
- * mcgb_batch_clock_tick(clock, n_sweeps, 1) in ONE launch: the CTA that
- * finishes the last replica of a ladder runs that ladder's exchange, and the
- * last cluster to finish advances the clock.  `sync` is n_ladders + 1 int32
- * counters, zero before the first call; every call leaves them zero.  Calls
- * sharing a `sync` array must not overlap on the GPU. */
+ * mcgb_batch_clock_tick(clock, n_sweeps, 1) in ONE launch: each pair of the
+ * matching is decided by the second of its two walkers to finish (with the
+ * same result as mcgb_batch_exchange), and the last cluster to finish
+ * advances the clock.  `sync` is 6 * n_replicas + 2 int32, 16-byte aligned,
+ * zero before the first call: per-slot posts and per-pair counts that run on
+ * from call to call, then a launch counter and an error flag.  One `sync`
+ * array per batch, kept for its lifetime; it may be zeroed (all of it)
+ * between calls.  Calls sharing it must not overlap on the GPU. */
 int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                int32_t *sync, void *stream);
 /* No counterpart in the reference.  n_windows consecutive windows of
@@ -312,18 +315,20 @@ int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb
  * RNG streams on chip between windows (loaded once, written back once).
  * Needs one cluster per replica (w->n_clusters == w->n_replicas, one replica
  * in every work list) and every cluster resident at once: otherwise the
- * launch fails (a CUDA error, MCGB_ECUDA) and nothing runs.  `sync` is
- * n_ladders + 3 int32: the counters of mcgb_batch_window_exchange, the window
- * epoch, and an error flag the kernel sets (and leaves set) if a wait between
- * windows gave up after about a second -- check it after the run.
+ * launch fails (a CUDA error, MCGB_ECUDA) and nothing runs.  Between
+ * windows each walker waits only for its own pair's decision.  `sync` is the
+ * array of mcgb_batch_window_exchange; its last entry is an error flag the
+ * kernel sets (and leaves set) if such a wait gave up after about a second:
+ * check it after the run.  After a failed launch the slot maps may disagree
+ * (t2w not the inverse of w2t): rebuild them and zero `sync` before going on.
  * n_windows = 1 is mcgb_batch_window_exchange. */
 int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                             int32_t *sync, int n_windows, void *stream);
 /* No counterpart in the reference.  Polls of a resident launch's wait
  * between windows before it gives up and raises the error flag (default
  * 2^22, about a second; negative restores the default).  Applies to later
- * calls; returns the previous value.  A small limit makes the waits run out,
- * which is how the timeout path is tested. */
+ * calls; returns the previous value.  With 0 every such wait gives up before
+ * its first poll, which is how the timeout path is tested. */
 int64_t mcgb_batch_set_wait_limit(int64_t polls);
 /* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
  * a captured graph of windows and exchanges can be replayed. */

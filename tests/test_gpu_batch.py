@@ -73,17 +73,35 @@ def test_ising_batch_pt_simulation_equals_dropin_simulation():
         np.testing.assert_array_equal(b.ladder_state(k), rt.snapshot())
 
 
-def test_graph_replay_equals_direct_launches():
+@pytest.mark.parametrize("resident", [True, False])
+def test_graph_replay_equals_direct_launches(resident):
+    """Replayed graphs (resident: ten windows per launch, each walker waiting
+    for its own pair only) against one fused launch per window, on ragged
+    ladders with unpaired end slots and a two-slot ladder: identical chains,
+    maps, betas, swap and round-trip counters and samples."""
     from mcgb.batch import LadderBatch
     from mcgb.models.xy.model import XYModel
-    kw = dict(seeds=[3], exchange_interval=5, proposal="gaussian", cluster_size=2, threads=256)
-    a = LadderBatch(XYModel(), [(32, np.geomspace(0.7, 1.2, 6))], **kw)
-    c = LadderBatch(XYModel(), [(32, np.geomspace(0.7, 1.2, 6))], **kw)
+    ladders = [(32, np.geomspace(0.7, 1.2, 6)), (16, [0.8, 1.0]), (16, [0.7, 0.9, 1.1])]
+    kw = dict(seeds=[3, 4, 5], exchange_interval=5, proposal="gaussian", cluster_size=2, threads=256)
+    a = LadderBatch(XYModel(), ladders, resident=resident, **kw)
+    c = LadderBatch(XYModel(), ladders, resident=False, **kw)
+    assert a.resident == resident
+    for b in (a, c):
+        b.allocate_samples(5, 5, 12)
     a.run(60, graph=True)
     c.run(60, graph=False)
-    np.testing.assert_array_equal(a.ladder_state(0), c.ladder_state(0))
-    np.testing.assert_array_equal(a.w2t.copy_to_host(), c.w2t.copy_to_host())
+    a.check_errors()
+    for k in range(len(ladders)):
+        np.testing.assert_array_equal(a.ladder_state(k), c.ladder_state(k))
+    for name in ("w2t", "t2w", "betas", "swap_counts", "trips", "energies", "clock", "samples"):
+        np.testing.assert_array_equal(getattr(a, name).copy_to_host(), getattr(c, name).copy_to_host(),
+                                      err_msg=name)
     np.testing.assert_array_equal(a.clock.copy_to_host(), [60, 12])
+    w2t, t2w = a.w2t.copy_to_host(), a.t2w.copy_to_host()
+    for s0, n in ((0, 6), (6, 2), (8, 3)):
+        np.testing.assert_array_equal(t2w[s0 + w2t[s0:s0 + n]], np.arange(n))
+    # 12 rounds: the 6-slot ladder alternates 3 and 2 pairs, the others 1
+    assert a.swap_counts.copy_to_host()[0].sum() == 6 * 3 + 6 * 2 + 12 + 12
 
 
 @pytest.mark.parametrize("proposal", ["uniform", "gaussian"])
@@ -399,10 +417,11 @@ def test_host_round_trip_resumes_the_chain_exactly():
 
 
 def test_resident_wait_that_runs_out_is_reported_and_the_batch_recovers():
-    """Failure detection: with a wait limit of zero polls the clusters of a
-    resident launch give up waiting for the window epoch at once; the kernel
-    raises its error flag and returns (no hang), check_errors() reports it as
-    MCGBTimeout and clears the counters, and later launches run normally."""
+    """Failure detection: with a wait limit of zero polls every walker of a
+    resident launch that waits for its pair's decision gives up at once; the
+    kernel raises its error flag and returns (no hang), check_errors()
+    reports it as MCGBTimeout, rebuilds consistent slot maps and clears the
+    counts, and later launches run normally."""
     from mcgb import _lib
     from mcgb.batch import LadderBatch
     from mcgb.models.xy.model import XYModel
@@ -419,6 +438,12 @@ def test_resident_wait_that_runs_out_is_reported_and_the_batch_recovers():
     finally:
         b.set_wait_limit(None)
     assert old == b.set_wait_limit(None)
+    w2t, t2w = b.w2t.copy_to_host(), b.t2w.copy_to_host()
+    np.testing.assert_array_equal(t2w[w2t], np.arange(4))
+    np.testing.assert_array_equal(b.betas.copy_to_host(), b._initial_betas[w2t])
+    assert not b.sync.copy_to_host().any()
     b.run(20)
     b.check_errors()
-    assert b.sync.copy_to_host().tolist() == [0] * (len(b.ladders) + 3)
+    w2t, t2w = b.w2t.copy_to_host(), b.t2w.copy_to_host()
+    np.testing.assert_array_equal(t2w[w2t], np.arange(4))
+    np.testing.assert_array_equal(b.betas.copy_to_host(), b._initial_betas[w2t])
