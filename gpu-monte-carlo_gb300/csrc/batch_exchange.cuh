@@ -1,7 +1,7 @@
 // Per-ladder replica exchange of the batched engine, as a block-cooperative
-// device function: the stand-alone exchange kernel runs it with one block per
-// ladder, and the fused window kernel runs it in the CTA that finishes a
-// ladder's last replica.
+// device function the stand-alone exchange kernel runs with one block per
+// ladder, and the bookkeeping of the fused window kernel, which decides the
+// same matching pair by pair (batch_window.cuh).
 #pragma once
 
 #include "batch_common.cuh"
@@ -227,19 +227,17 @@ __device__ __forceinline__ void exchange_ladder(const ExchangeArgs &x, int l)
 }
 
 // Bookkeeping of the fused window + exchange launch, carved out of one int32
-// array `sync` of 6 * n_replicas + 2 entries (16-byte aligned, zero before
-// the first launch; the pair counts run on from launch to launch):
-//   post     [n_replicas] x 16 B  per global temperature slot: the energy
-//                                 (double), then beta (float bits, low word)
-//                                 and the local walker id (high word) of the
-//                                 walker that last finished at that slot
-//   arrive   [n_replicas]         per pair, at its left slot: walkers counted
-//   decided  [n_replicas]         per pair: (round + 1) << 1 | swapped
+// array `sync` of 5 * n_replicas + 2 entries (16-byte aligned, zero before
+// the first launch):
+//   mailbox [n_replicas] x 16 B  per pair, at its left global slot: empty
+//                                (zero) or the first walker's post -- energy
+//                                (double), then beta (float bits, low word)
+//                                and 0x80000000 | local walker id (high word)
+//   decided [n_replicas]         per pair: (round tag << 1) | swapped
 //   launch_done [1], error [1]
 struct FusedExchange {
     ExchangeArgs ex;
-    double2 *post;
-    unsigned *arrive;
+    double2 *mailbox;
     int32_t *decided;
     int32_t *launch_done;
     int32_t *error;        // set when a wait for a pair's decision gave up
@@ -248,18 +246,15 @@ struct FusedExchange {
     long long wait_limit;  // polls of a pair's decision before a wait gives up
 };
 
-__host__ __device__ inline long long fused_sync_words(int n_replicas) { return 6ll * n_replicas + 2; }
-
 inline FusedExchange make_fused(const ExchangeArgs &ex, int32_t *sync, int n_windows, long long wait_limit)
 {
     const int n = ex.n_replicas;
     FusedExchange fx;
     fx.ex = ex;
-    fx.post = reinterpret_cast<double2 *>(sync);
-    fx.arrive = reinterpret_cast<unsigned *>(sync + 4ll * n);
-    fx.decided = sync + 5ll * n;
-    fx.launch_done = sync + 6ll * n;
-    fx.error = sync + 6ll * n + 1;
+    fx.mailbox = reinterpret_cast<double2 *>(sync);
+    fx.decided = sync + 4ll * n;
+    fx.launch_done = sync + 5ll * n;
+    fx.error = sync + 5ll * n + 1;
     fx.enabled = 1;
     fx.n_windows = n_windows;
     fx.wait_limit = wait_limit;

@@ -166,6 +166,7 @@ extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w,
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
     if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
     MCGB_REQUIRE((reinterpret_cast<uintptr_t>(sync) & 15) == 0, "window_exchange: sync must be 16-byte aligned");
+    MCGB_REQUIRE(pt->channels <= 32, "window_exchange: at most 32 sample channels");
     const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, 1, kWaitSpinLimit);
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
@@ -194,6 +195,7 @@ extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, co
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
     if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
     MCGB_REQUIRE((reinterpret_cast<uintptr_t>(sync) & 15) == 0, "run_resident: sync must be 16-byte aligned");
+    MCGB_REQUIRE(pt->channels <= 32, "run_resident: at most 32 sample channels");
     const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, n_windows, g_wait_limit);
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);

@@ -428,116 +428,169 @@ __device__ __forceinline__ int load_acquire(const int32_t *p)
 // window's length.
 constexpr long long kWaitSpinLimit = 1ll << 22;
 
-// The fused replica exchange of walker r after window `win` of a launch of
-// n_windows: core/parallel_tempering.py:35-91, decided pair by pair as soon
-// as both walkers of a pair are done, so no walker waits for the rest of its
-// ladder.  Lane 0 of the walker's rank-0 warp 0 posts (energy, beta, id) at
-// the walker's slot and counts it at its pair; the second to arrive decides
-// with the pair's stream and writes the swap counters, maps and betas of
-// both.  Between the windows of a resident launch the first to arrive waits
-// for that decision, bounded: on giving up it raises the error flag and
-// keeps its slot (the host then reports the launch as failed).  After the
-// last window nobody waits: the decider settles both walkers.  Every round
-// brings exactly two arrivals to each of its pairs, and a walker reaches a
-// pair's next round only after that pair's decision, so the arrival count
-// names the round and a decision word cannot be mistaken for an earlier one.
-// Settling a walker at its new slot -- round-trip counters and the staged
-// window-end sample -- is spread over the warp.  Decisions, maps, counters,
+// 16-byte atomic exchange with acquire-release semantics at GPU scope
+// (PTX atom.exch.b128, sm_90 and later): stores (lo, hi) at p, returns the
+// previous contents.
+__device__ __forceinline__ void exchange16(double2 *p, unsigned long long lo, unsigned long long hi,
+                                           unsigned long long &old_lo, unsigned long long &old_hi)
+{
+    asm volatile(
+        "{\n\t.reg .b128 nv, ov;\n\t"
+        "mov.b128 nv, {%2, %3};\n\t"
+        "atom.acq_rel.gpu.global.exch.b128 ov, [%4], nv;\n\t"
+        "mov.b128 {%0, %1}, ov;\n\t}"
+        : "=l"(old_lo), "=l"(old_hi)
+        : "l"(lo), "l"(hi), "l"(p)
+        : "memory");
+}
+
+__device__ __forceinline__ void store_release(int32_t *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The exchange acceptance of core/parallel_tempering.py:76-80 for a draw u
+// in (0, 1) and log_ratio < 0: log(u) < log_ratio, decided exactly as in
+// double precision.  A float logf settles all but a sliver of cases: with
+// u rounded to float (relative error 2^-24, so log moves by under 6.0e-8)
+// and logf within a few ulp (under 3 * 2^-18 = 1.2e-5 for |log| < 37, the
+// range of 53-bit draws), the float result lies within 1e-5 * (1 + |lr|) of
+// log(u); only inside that margin is the double log computed.
+__device__ __forceinline__ bool exchange_accepts(double u, double log_ratio)
+{
+    const float lf = logf((float)u);
+    const double margin = 1e-5 * (1.0 - log_ratio);
+    if ((double)lf < log_ratio - margin) return true;
+    if ((double)lf > log_ratio + margin) return false;
+    return log(u) < log_ratio;
+}
+
+// The fused replica exchange of walker r (slot s, beta b, energy e) after
+// the window that ends at sweep `sweep`, the exchange round after `rounds`
+// earlier ones, with the window-end sample staged for ring slot `slot` (-1:
+// none) and `wait` when more windows follow in this launch:
+// core/parallel_tempering.py:35-91, decided pair by pair as soon as both
+// walkers of a pair are done, so no walker waits for the rest of its
+// ladder.  Lane 0 of the walker's rank-0 warp 0 swaps its post into the
+// pair's mailbox in one atomic: finding it empty, the walker is first;
+// finding the partner's post, it decides with the pair's stream, empties the
+// mailbox and writes the swap counters, maps, betas and (released) the
+// decision word of both.  Between the windows of a resident launch the first
+// walker waits for that word, bounded: on giving up it raises the error flag
+// and keeps its slot (the host then reports the launch as failed).  After
+// the last window nobody waits: the decider settles both walkers.  A walker
+// reaches a pair's next round only after the pair's decision, so the mailbox
+// is empty at every round's first arrival, and the word carries the round's
+// tag (the exchange-round count + 1).  The other lanes load the walker's
+// staged sample and round-trip counters (and the pair's stream) meanwhile;
+// settling them at the new slot is then stores.  Decisions, maps, counters,
 // round trips and sample slots are exchange_ladder's on the same window.
 // Called by the 32 threads of warp 0; kept light in registers, because the
 // window kernel keeps its sweep state live across the call.
-static __device__ __noinline__ void pair_finished(const FusedExchange &fx, const mcgb_replica &rep, int r, int win,
-                                                  int n_windows)
+static __device__ __noinline__ void pair_finished(const FusedExchange &fx, const mcgb_replica &rep, int r, int s,
+                                                  float b, double e, long long sweep, long long rounds, int slot,
+                                                  bool wait)
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const ExchangeArgs &x = fx.ex;
-    const int start = rep.ladder_start, R = rep.n_temps, w = r - start;
-    const long long sweep = __ldcg(x.clock) + (long long)(win + 1) * x.window_sweeps;
-    const bool wait = win + 1 < n_windows;
+    const int start = rep.ladder_start, R = rep.n_temps, w = r - start, n = x.n_replicas;
+    const int parity = R > 2 ? (int)(rounds & 1) : 0;
+    int left = -1;
+    if (R >= 2) {
+        if (s >= parity && ((s - parity) & 1) == 0 && s < R - 1)
+            left = s;
+        else if (s >= 1 + parity && ((s - 1 - parity) & 1) == 0)
+            left = s - 1;
+    }
+    const int partner = left < 0 ? s : (s == left ? left + 1 : left);
+    const int poff = start - rep.ladder;
+    const int tag = (int)((rounds + 1) & 0x3fffffff);
+    double2 *box = fx.mailbox + start + (left < 0 ? 0 : left);
+
+    // Loads that do not depend on the decision, off lane 0.
+    double own = 0.0;  // lane q < channels: channel q of the staged sample
+    if (slot >= 0 && lane < x.channels) own = __ldcg(x.staging + (size_t)lane * n + r);
+    long long *tr = x.trips + r;
+    const bool ends = s == 0 || s == R - 1 || partner == 0 || partner == R - 1;
+    long long origin = 0, visited = 0, sweep0 = 0, ntrips = 0, tsweeps = 0;  // lane 1
+    if (lane == 1 && ends) {
+        origin = __ldcg(tr);
+        visited = __ldcg(tr + n);
+        sweep0 = __ldcg(tr + 2 * n);
+        ntrips = __ldcg(tr + 3 * n);
+        tsweeps = __ldcg(tr + 4 * n);
+    }
+    // The pair's stream (lane 2): its last writer decided the pair's previous
+    // round, which this walker's own rounds have ordered before this load.
+    ulonglong2 st = make_ulonglong2(0, 0);
+    if (lane == 2 && left >= 0) st = __ldcg(x.rng + poff + left);
+    // Lane 0 posts; the stream travels to it while the atomic is in flight.
+    unsigned long long got_lo = 0, got_hi = 0;
+    if (lane == 0 && left >= 0)
+        exchange16(box, (unsigned long long)__double_as_longlong(e),
+                   (1ull << 63) | ((unsigned long long)(unsigned)w << 32) | __float_as_uint(b), got_lo, got_hi);
+    st.x = __shfl_sync(full, st.x, 2);
+    st.y = __shfl_sync(full, st.y, 2);
+
     // walker w ends at slot t0 (-1: unknown); walker w1 (-1: none) at t1
     int t0 = -1, w1 = -1, t1 = -1;
     if (lane == 0) {
-        const int parity = R > 2 ? (int)((__ldcg(x.clock + 1) + win) & 1) : 0;
-        const int s = __ldcg(x.w2t + r);
-        int left = -1;
-        if (R >= 2) {
-            if (s >= parity && ((s - parity) & 1) == 0 && s < R - 1)
-                left = s;
-            else if (s >= 1 + parity && ((s - 1 - parity) & 1) == 0)
-                left = s - 1;
-        }
         if (left < 0) {
             t0 = s;  // no partner this round
-        } else {
-            const int partner = s == left ? left + 1 : left;
-            const double e = __ldcg(x.energies + r);
-            const float b = __ldcg(x.betas + r);
-            const unsigned long long tag = ((unsigned long long)(unsigned)w << 32) | __float_as_uint(b);
-            fx.post[start + s] = make_double2(e, __longlong_as_double((long long)tag));
-            __threadfence();
-            const unsigned old = atomicAdd(fx.arrive + start + left, 1u);
-            const int round = (int)(((old >> 1) + 1u) & 0x3fffffffu);
-            if (old & 1u) {
-                __threadfence();
-                const int poff = start - rep.ladder, np = x.n_pairs_total;
-                const double2 q = __ldcg(fx.post + start + partner);
-                long long *cnt = x.counts + poff + left;
-                long long att = __ldcg(cnt), acc = __ldcg(cnt + np), nonf = __ldcg(cnt + 2 * np);
-                ulonglong2 st = __ldcg(x.rng + poff + left);
-                const unsigned long long qtag = (unsigned long long)__double_as_longlong(q.y);
-                const int wq = (int)(qtag >> 32);
-                const float bq = __uint_as_float((unsigned)qtag);
-                const bool me_left = s == left;
-                const double ea = me_left ? e : q.x, eb = me_left ? q.x : e;
-                const float ba = me_left ? b : bq, bb = me_left ? bq : b;
-                int swapped = 0;
-                att += 1;
-                if (!isfinite(ea) || !isfinite(eb)) {
-                    nonf += 1;
-                } else {
-                    const double log_ratio = ((double)ba - (double)bb) * (ea - eb);
-                    const double u = xoro_uniform_f64(st);
-                    x.rng[poff + left] = st;
-                    if (log_ratio >= 0.0 || u == 0.0 || log(u) < log_ratio) {
-                        swapped = 1;
-                        acc += 1;
-                    }
+        } else if (got_hi >> 63) {
+            // Second to arrive: decide.
+            const int wq = (int)((got_hi >> 32) & 0x7fffffffu);
+            const double eq = __longlong_as_double((long long)got_lo);
+            const float bq = __uint_as_float((unsigned)got_hi);
+            const bool me_left = s == left;
+            const double ea = me_left ? e : eq, eb = me_left ? eq : e;
+            const float ba = me_left ? b : bq, bb = me_left ? bq : b;
+            const int np = x.n_pairs_total;
+            unsigned long long *cnt = reinterpret_cast<unsigned long long *>(x.counts + poff + left);
+            int swapped = 0;
+            atomicAdd(cnt, 1ull);
+            if (!isfinite(ea) || !isfinite(eb)) {
+                atomicAdd(cnt + 2 * np, 1ull);
+            } else {
+                const double log_ratio = ((double)ba - (double)bb) * (ea - eb);
+                const double u = xoro_uniform_f64(st);
+                x.rng[poff + left] = st;
+                if (log_ratio >= 0.0 || u == 0.0 || exchange_accepts(u, log_ratio)) {
+                    swapped = 1;
+                    atomicAdd(cnt + np, 1ull);
                 }
-                cnt[0] = att;
-                cnt[np] = acc;
-                cnt[2 * np] = nonf;
-                if (swapped) {
-                    const int wa = me_left ? w : wq, wb = me_left ? wq : w;
-                    x.t2w[start + left] = wb;
-                    x.t2w[start + left + 1] = wa;
-                    x.w2t[start + wa] = left + 1;
-                    x.w2t[start + wb] = left;
-                    x.betas[start + wa] = bb;
-                    x.betas[start + wb] = ba;
+            }
+            if (swapped) {
+                const int wa = me_left ? w : wq, wb = me_left ? wq : w;
+                x.t2w[start + left] = wb;
+                x.t2w[start + left + 1] = wa;
+                x.w2t[start + wa] = left + 1;
+                x.w2t[start + wb] = left;
+                x.betas[start + wa] = bb;
+                x.betas[start + wb] = ba;
+            }
+            *box = make_double2(0.0, 0.0);
+            store_release(fx.decided + start + left, tag << 1 | swapped);
+            t0 = swapped ? partner : s;
+            if (!wait) {
+                w1 = wq;
+                t1 = swapped ? s : partner;
+            }
+        } else if (wait) {
+            unsigned ns = 32;
+            for (long long it = 0;; ++it) {
+                if (it >= fx.wait_limit) {
+                    atomicExch(fx.error, 1);
+                    break;
                 }
-                __threadfence();
-                atomicExch(fx.decided + start + left, round << 1 | swapped);
-                t0 = swapped ? partner : s;
-                if (!wait) {
-                    w1 = wq;
-                    t1 = swapped ? s : partner;
+                const int v = load_acquire(fx.decided + start + left);
+                if ((v >> 1) == tag) {
+                    t0 = (v & 1) ? partner : s;
+                    break;
                 }
-            } else if (wait) {
-                unsigned ns = 32;
-                for (long long it = 0;; ++it) {
-                    if (it >= fx.wait_limit) {
-                        atomicExch(fx.error, 1);
-                        break;
-                    }
-                    const int v = load_acquire(fx.decided + start + left);
-                    if ((v >> 1) == round) {
-                        t0 = (v & 1) ? partner : s;
-                        break;
-                    }
-                    __nanosleep(ns);
-                    if (ns < 256) ns <<= 1;
-                }
+                __nanosleep(ns);
+                if (ns < 256) ns <<= 1;
             }
         }
     }
@@ -545,35 +598,38 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, const
     w1 = __shfl_sync(full, w1, 0);
     t1 = __shfl_sync(full, t1, 0);
     __syncwarp();  // orders lane 0's acquire before the other lanes' reads
-    // Settle: lane k < 2 keeps walker k's round-trip counters, then the lanes
-    // copy the staged sample channels to the walkers' new slots.
-    const int wk = lane == 0 ? w : w1, tk = lane == 0 ? t0 : t1;
-    const int n = x.n_replicas;
-    if (lane < 2 && tk >= 0 && (tk == 0 || tk == R - 1)) {
-        long long *tr = x.trips + start + wk;
-        const long long origin = __ldcg(tr), visited = __ldcg(tr + n), sweep0 = __ldcg(tr + 2 * n),
-                        ntrips = __ldcg(tr + 3 * n), tsweeps = __ldcg(tr + 4 * n);
-        if (origin < 0) {
-            tr[0] = tk;
-            tr[2 * n] = sweep;
-        } else if (tk != origin) {
-            tr[n] = 1;
-        } else if (visited) {
-            tr[3 * n] = ntrips + 1;
-            tr[4 * n] = tsweeps + (sweep - sweep0);
-            tr[2 * n] = sweep;
-            tr[n] = 0;
+
+    // Settle: round-trip counters (lane 1 for this walker, lane 3 for the
+    // partner the decider settles), then the staged samples at the new slots.
+    if ((lane == 1 && t0 >= 0 && ends) || (lane == 3 && t1 >= 0)) {
+        const int t = lane == 1 ? t0 : t1;
+        if (lane == 3) {
+            tr = x.trips + start + w1;
+            origin = __ldcg(tr);
+            visited = __ldcg(tr + n);
+            sweep0 = __ldcg(tr + 2 * n);
+            ntrips = __ldcg(tr + 3 * n);
+            tsweeps = __ldcg(tr + 4 * n);
+        }
+        if (t == 0 || t == R - 1) {
+            if (origin < 0) {
+                tr[0] = t;
+                tr[2 * n] = sweep;
+            } else if (t != origin) {
+                tr[n] = 1;
+            } else if (visited) {
+                tr[3 * n] = ntrips + 1;
+                tr[4 * n] = tsweeps + (sweep - sweep0);
+                tr[2 * n] = sweep;
+                tr[n] = 0;
+            }
         }
     }
-    if (x.staging == nullptr || x.samples == nullptr) return;
-    const int slot = sample_slot(sweep, x.first_sample_sweep, x.sample_interval, x.n_slots);
     if (slot < 0) return;
     double *out = x.samples + (size_t)slot * x.channels * x.n_temps_total + start;
-    for (int j = lane; j < 2 * x.channels; j += 32) {
-        const int k = j < x.channels ? 0 : 1, q = j - k * x.channels;
-        const int wj = k ? w1 : w, tj = k ? t1 : t0;
-        if (tj >= 0) out[(size_t)q * x.n_temps_total + tj] = __ldcg(x.staging + (size_t)q * n + start + wj);
-    }
+    if (t0 >= 0 && lane < x.channels) out[(size_t)lane * x.n_temps_total + t0] = own;
+    if (t1 >= 0 && lane < x.channels)
+        out[(size_t)lane * x.n_temps_total + t1] = __ldcg(x.staging + (size_t)lane * n + start + w1);
 }
 
 // Threads per block the NPMAX variant is compiled for: NPMAX streams of four
@@ -670,6 +726,17 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         const int tslot = rep.ladder_start + __ldcg(cm.w2t + r);
         cluster_arrive();
 
+        // This window's sample schedule (sample_slot's, stepped without
+        // divisions): the next sweep number due a sample and its ring slot.
+        long long next_sample = -1;
+        int next_slot = 0;
+        if (cm.samples != nullptr && cm.sample_interval > 0 && cm.n_slots > 0) {
+            const long long first = cm.first_sample_sweep, from = sweep0 + 1;
+            const long long k = from <= first ? 0 : (from - first + cm.sample_interval - 1) / cm.sample_interval;
+            next_sample = first + k * cm.sample_interval;
+            next_slot = (int)(k % cm.n_slots);
+        }
+
         float dsum = 0.0f, dcomp = 0.0f;
         int nacc = 0;
         // A sample whose partial sums wait in rank 0's `parts`: -1 none, -2
@@ -748,8 +815,10 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
 
             comp_add(dsum, dcomp, dacc);
-            const int slot = sample_slot(sweep0 + s + 1, cm.first_sample_sweep, cm.sample_interval, cm.n_slots);
-            if (slot >= 0 && cm.samples != nullptr) {
+            if (sweep0 + s + 1 == next_sample) {
+                const int slot = next_slot;
+                next_sample += cm.sample_interval;
+                next_slot = next_slot + 1 == cm.n_slots ? 0 : next_slot + 1;
                 // Measure the strip, reduce over the CTA, push the partial
                 // sums into rank 0 ahead of the barrier that ends this phase.
                 cluster_wait();
@@ -758,9 +827,19 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 cluster_arrive();
             }
         }
+        // Ring slot of a sample staged on the window's last sweep (-1: none).
+        const int end_slot = pend == -2 ? (next_slot == 0 ? cm.n_slots - 1 : next_slot - 1) : -1;
         cluster_wait();
         MCGB_COMBINE_PENDING()
 #undef MCGB_COMBINE_PENDING
+        // Loaded ahead of the epilogue: the acceptance count, and for the
+        // exchange the walker's beta and the exchange rounds before this one.
+        const long long acc_prev = rank == 0 && tid == 0 ? __ldcg(cm.accepted + r) : 0;
+        const float beta_now = a.fx.enabled && rank == 0 && tid == 0 ? __ldcg(cm.betas + r) : 0.0f;
+        const long long rounds = a.fx.enabled && rank == 0 && tid < 32 ? __ldcg(cm.clock + 1) + win : 0;
+        double e_now = 0.0;
+        float e_hi = 0.0f, e_lo = 0.0f;
+        long long acc_now = 0;
 
         // Window epilogue: energy and acceptance bookkeeping (compensated
         // float32 partial sums pushed into rank 0, as for samples), write back.
@@ -799,7 +878,6 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         }
         cluster.sync();
         if (rank == 0 && tid == 0) {
-            double e_now;
             FSum de, na, ex;
             for (int k = 0; k < C; ++k) {
                 const float2 *pk = parts + k * NP + NS;
@@ -821,13 +899,21 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 two_sum(s1, lo, hi, lo2);
                 e_now = (double)hi + (double)lo2;
             }
-            cm.energies[r] = e_now;
-            cm.e_run[2 * r] = hi;
-            cm.e_run[2 * r + 1] = lo2;
-            cm.accepted[r] = __ldcg(cm.accepted + r) + (long long)na.value();
+            e_hi = hi;
+            e_lo = lo2;
+            acc_now = acc_prev + (long long)na.value();
         }
         __syncwarp();
-        if (a.fx.enabled && rank == 0 && tid < 32) pair_finished(a.fx, rep, r, win, n_windows);
+        if (a.fx.enabled && rank == 0 && tid < 32)
+            pair_finished(a.fx, rep, r, tslot - rep.ladder_start, beta_now, e_now, sweep0 + cm.n_sweeps, rounds,
+                          end_slot, win + 1 < n_windows);
+        // After the exchange, whose releasing atomic need not wait for them.
+        if (rank == 0 && tid == 0) {
+            cm.energies[r] = e_now;
+            cm.e_run[2 * r] = e_hi;
+            cm.e_run[2 * r + 1] = e_lo;
+            cm.accepted[r] = acc_now;
+        }
         __syncwarp();  // the aligned cluster barrier needs warp 0 converged again
         cluster.sync();
         }  // windows

@@ -269,10 +269,10 @@ class LadderBatch:
                 pair_rng[po:po + n - 1].raw().copy_(sub.raw())
             self.pair_rng = pair_rng
             self.swap_counts = device_zeros((3, n_pairs), np.int64)
-            # Bookkeeping of the fused window + exchange launch: per-slot
-            # posts (4 words each), per-pair arrival counts and decisions,
-            # the launch counter, then the error flag.
-            self.sync = device_zeros(6 * self.R + 2, np.int32)
+            # Bookkeeping of the fused window + exchange launch: per-pair
+            # mailboxes (4 words each) and decision words, the launch
+            # counter, then the error flag.
+            self.sync = device_zeros(5 * self.R + 2, np.int32)
             trips = np.zeros((5, self.R), np.int64)
             trips[0] = -1
             trips[2] = -1

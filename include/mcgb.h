@@ -302,11 +302,12 @@ int mcgb_batch_window_exchange_noalloc(int model, const mcgb_batch_window *w, co
  * mcgb_batch_clock_tick(clock, n_sweeps, 1) in ONE launch: each pair of the
  * matching is decided by the second of its two walkers to finish (with the
  * same result as mcgb_batch_exchange), and the last cluster to finish
- * advances the clock.  `sync` is 6 * n_replicas + 2 int32, 16-byte aligned,
- * zero before the first call: per-slot posts and per-pair counts that run on
- * from call to call, then a launch counter and an error flag.  One `sync`
- * array per batch, kept for its lifetime; it may be zeroed (all of it)
- * between calls.  Calls sharing it must not overlap on the GPU. */
+ * advances the clock.  At most 32 sample channels.  `sync` is
+ * 5 * n_replicas + 2 int32, 16-byte aligned, zero before the first call:
+ * per-pair mailboxes and decision words (tagged with the exchange-round
+ * count clock[1]), a launch counter and an error flag.  One `sync` array per
+ * batch, kept for its lifetime; zero all of it if clock[1] is ever set back.
+ * Calls sharing it must not overlap on the GPU. */
 int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                int32_t *sync, void *stream);
 /* No counterpart in the reference.  n_windows consecutive windows of
