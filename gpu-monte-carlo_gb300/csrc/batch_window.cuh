@@ -147,11 +147,16 @@ __host__ __device__ constexpr int part_slots()
     return M::kSums + 3;
 }
 
+// A copy of the launch's exchange arguments in shared memory, read once per
+// window by the exchange (its lines in the parameter bank go cold over a
+// window's sweeps).
+constexpr size_t kFusedCopyBytes = (sizeof(FusedExchange) + 15) & ~static_cast<size_t>(15);
+
 // Shared memory of a strip with npl plaquettes in rows of lp.
 template <class M>
 __host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp)
 {
-    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * part_slots<M>()) +
+    return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * part_slots<M>()) + kFusedCopyBytes +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
            (size_t)4 * npl * sizeof(float) * M::kOwnFloats;
 }
@@ -465,7 +470,9 @@ __device__ __forceinline__ bool exchange_accepts(double u, double log_ratio)
     return log(u) < log_ratio;
 }
 
-// The fused replica exchange of walker r (slot s, beta b, energy e) after
+// The fused replica exchange of walker r (slot s, beta b, energy e) of the
+// ladder of R slots from global slot `start` (ladder index `ladder`), with
+// `fx` the shared-memory copy of the exchange arguments, after
 // the window that ends at sweep `sweep`, the exchange round after `rounds`
 // earlier ones, with the window-end sample staged for ring slot `slot` (-1:
 // none) and `wait` when more windows follow in this launch:
@@ -487,14 +494,14 @@ __device__ __forceinline__ bool exchange_accepts(double u, double log_ratio)
 // round trips and sample slots are exchange_ladder's on the same window.
 // Called by the 32 threads of warp 0; kept light in registers, because the
 // window kernel keeps its sweep state live across the call.
-static __device__ __noinline__ void pair_finished(const FusedExchange &fx, const mcgb_replica &rep, int r, int s,
-                                                  float b, double e, long long sweep, long long rounds, int slot,
-                                                  bool wait)
+static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int start, int R, int ladder, int r,
+                                                  int s, float b, double e, long long sweep, long long rounds,
+                                                  int slot, bool wait)
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const ExchangeArgs &x = fx.ex;
-    const int start = rep.ladder_start, R = rep.n_temps, w = r - start, n = x.n_replicas;
+    const int w = r - start, n = x.n_replicas;
     const int parity = R > 2 ? (int)(rounds & 1) : 0;
     int left = -1;
     if (R >= 2) {
@@ -504,7 +511,7 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, const
             left = s - 1;
     }
     const int partner = left < 0 ? s : (s == left ? left + 1 : left);
-    const int poff = start - rep.ladder;
+    const int poff = start - ladder;
     const int tag = (int)((rounds + 1) & 0x3fffffff);
     double2 *box = fx.mailbox + start + (left < 0 ? 0 : left);
 
@@ -661,10 +668,12 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     double *scratch = red + kRedDoubles;               // 32 * (NS + 3)
     constexpr int NP = part_slots<M>();
     float2 *parts = reinterpret_cast<float2 *>(scratch + 32 * (NS + 3));  // [kMaxCluster][NP], rank 0's used
-    Cell *cells = reinterpret_cast<Cell *>(parts + kMaxCluster * NP);
+    FusedExchange *fxs = reinterpret_cast<FusedExchange *>(parts + kMaxCluster * NP);
+    Cell *cells = reinterpret_cast<Cell *>(reinterpret_cast<unsigned char *>(fxs) + kFusedCopyBytes);
 
     const WindowCommon &cm = a.c;
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
+    if (a.fx.enabled && tid == 0) *fxs = a.fx;
     // DSMEM stores below need every CTA of the cluster to be running.
     cluster.sync();
 
@@ -905,8 +914,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         }
         __syncwarp();
         if (a.fx.enabled && rank == 0 && tid < 32)
-            pair_finished(a.fx, rep, r, tslot - rep.ladder_start, beta_now, e_now, sweep0 + cm.n_sweeps, rounds,
-                          end_slot, win + 1 < n_windows);
+            pair_finished(*fxs, rep.ladder_start, rep.n_temps, rep.ladder, r, tslot - rep.ladder_start, beta_now,
+                          e_now, sweep0 + cm.n_sweeps, rounds, end_slot, win + 1 < n_windows);
         // After the exchange, whose releasing atomic need not wait for them.
         if (rank == 0 && tid == 0) {
             cm.energies[r] = e_now;
