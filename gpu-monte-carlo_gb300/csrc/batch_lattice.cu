@@ -158,8 +158,9 @@ struct XYPolicy {
         static_cast<float *>(a.state)[site] = own[0];
         a.aux[site] = cell;
     }
-    // Draws (in order): Gaussian (u1, u2) from one draw, accept v; uniform
-    // u, accept v.  The mixed form uses 23-bit uniforms (mcgb_fast_unit).
+    // Draws: Gaussian -- one draw, its three visit uniforms (u1, u2, v;
+    // mcgb_visit_*); uniform -- u, then the acceptance v (23-bit
+    // mcgb_fast_unit in the mixed form).
     template <int C_>
     static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &, const float *own, ulonglong2 &st)
     {
@@ -168,9 +169,8 @@ struct XYPolicy {
         Prop q;
         if (x.gauss) {
             const uint64_t bits = xoro_next(st);
-            float u1 = mcgb_fast_unit(bits);
-            const float u2 = mcgb_fast_unit_mid(bits);
-            if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
+            const float u1 = mcgb_visit_u1(bits), u2 = mcgb_visit_u2(bits);
+            q.v = mcgb_visit_v(bits);
             const float t2 = -2.0f * __logf(u1);
             // cos(2 pi u2) = -cos(2 pi u2 - pi), evaluated on [-pi, pi].
             const float z = -(t2 * rsqrtf(t2)) * __cosf(fmaf(two_pi, u2, -pi));
@@ -185,9 +185,9 @@ struct XYPolicy {
             if (tp >= pi) tp -= two_pi;
             else if (tp < -pi) tp += two_pi;
             q.tp = tp;
+            q.v = mcgb_fast_unit(xoro_next(st));
         }
         __sincosf(q.tp, &q.sp, &q.cp);
-        q.v = mcgb_fast_unit(xoro_next(st));
         return q;
     }
     template <int C_>

@@ -136,19 +136,19 @@ __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restric
     const float th = b[i * L + j];
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
     ulonglong2 st = rng[idx];
-    float proposed;
+    float proposed, v;
     if (!kGauss) {
         const float u = xoro_uniform_f32(st);
         proposed = th + delta * (2.0f * u - 1.0f);
         // delta <= pi and theta in [-pi, pi): one wrap suffices.
         if (proposed >= pi) proposed -= two_pi;
         else if (proposed < -pi) proposed += two_pi;
+        v = xoro_uniform_f32(st);
     } else {
-        // Two draws per visit: u1, u2 from bits 63..41 and 40..18 of one.
+        // One draw per visit: u1, u2 and the acceptance v (mcgb_visit_*).
         const uint64_t x = xoro_next(st);
-        float u1 = mcgb_fast_unit(x);
-        const float u2 = mcgb_fast_unit_mid(x);
-        if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
+        const float u1 = mcgb_visit_u1(x), u2 = mcgb_visit_u2(x);
+        v = mcgb_visit_v(x);
         const float z = sqrtf(-2.0f * logf(u1)) * cosf(two_pi * u2);
         proposed = th + sigmas[r] * z;
         proposed -= two_pi * floorf((proposed + pi) / two_pi);
@@ -158,7 +158,6 @@ __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restric
     const float e_old = -J * xy_bond_sum(b, L, i, j, th);
     const float e_new = -J * xy_bond_sum(b, L, i, j, proposed);
     const float dE = e_new - e_old;
-    const float v = xoro_uniform_f32(st);
     rng[idx] = st;
     if (dE <= 0.0f || v < expf(-betas[r] * dE)) b[i * L + j] = proposed;
 }

@@ -136,3 +136,25 @@ MCGB_HD float mcgb_fast_unit_mid(uint64_t x)
 {
     return mcgb_bits_to_float(0x3f800000u | ((uint32_t)(x >> 18) & 0x7fffffu)) - 1.0f;
 }
+
+// The three uniforms of a Gaussian Metropolis visit of an XY spin, all from
+// one draw x (each exact in float32):
+//   u1 = (2k + 1) 2^-22, k = bits 63..43  -- strictly inside (0, 1), the
+//        Box-Muller radius draw (no logarithm of zero, no clamp);
+//   u2 = k 2^-21,        k = bits 42..22  -- the Box-Muller angle draw;
+//   v  = k 2^-21,        k = bits 21..1   -- the acceptance draw (bit 0, the
+//        generator's weakest, unused).
+// The proposal is a Gaussian truncated at 5.4 sigma on a 2^-21 grid,
+// symmetric, so Metropolis acceptance keeps detailed balance.
+MCGB_HD float mcgb_visit_u1(uint64_t x)
+{
+    return mcgb_bits_to_float(0x3f800000u | ((uint32_t)(x >> 43) << 2) | 2u) - 1.0f;
+}
+MCGB_HD float mcgb_visit_u2(uint64_t x)
+{
+    return mcgb_bits_to_float(0x3f800000u | (((uint32_t)(x >> 22) & 0x1fffffu) << 2)) - 1.0f;
+}
+MCGB_HD float mcgb_visit_v(uint64_t x)
+{
+    return mcgb_bits_to_float(0x3f800000u | (((uint32_t)(x >> 1) & 0x1fffffu) << 2)) - 1.0f;
+}

@@ -223,17 +223,20 @@ static void xy_color_replica(float *theta, uint64_t *rng, float beta, int r, int
             float t = b[i * L + j];
             int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
             uint64_t *st = rng + 2 * idx;
-            float proposed;
+            float proposed, v;
             if (!gaussian) {
                 float u = orc_rng_uniform_f32(st);
                 proposed = t + delta * (2.0f * u - 1.0f);
                 if (proposed >= PI_F) proposed -= TWO_PI_F;
                 else if (proposed < -PI_F) proposed += TWO_PI_F;
+                v = orc_rng_uniform_f32(st);
             } else {
+                /* one draw per visit: u1 = (2k+1) 2^-22 (bits 63..43), u2 = k 2^-21
+                   (bits 42..22), acceptance v = k 2^-21 (bits 21..1) */
                 uint64_t x = orc_rng_next(st);
-                float u1 = (float)(x >> 41) * 0x1p-23f;
-                float u2 = (float)((x >> 18) & 0x7fffffu) * 0x1p-23f;
-                if (u1 <= 0.0f) u1 = 1.1102230246251565e-16f;
+                float u1 = (float)(2u * (uint32_t)(x >> 43) + 1u) * 0x1p-22f;
+                float u2 = (float)((uint32_t)(x >> 22) & 0x1fffffu) * 0x1p-21f;
+                v = (float)((uint32_t)(x >> 1) & 0x1fffffu) * 0x1p-21f;
                 float z = sqrtf(-2.0f * logf(u1)) * cosf(TWO_PI_F * u2);
                 proposed = t + sigma * z;
                 proposed -= TWO_PI_F * floorf((proposed + PI_F) / TWO_PI_F);
@@ -243,7 +246,6 @@ static void xy_color_replica(float *theta, uint64_t *rng, float beta, int r, int
             float e_old = -J * xy_bond_sum(b, L, i, j, t);
             float e_new = -J * xy_bond_sum(b, L, i, j, proposed);
             float dE = e_new - e_old;
-            float v = orc_rng_uniform_f32(st);
             if (dE <= 0.0f || v < expf(-beta * dE)) b[i * L + j] = proposed;
         }
 }
