@@ -327,17 +327,47 @@ __device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, typen
     }
 }
 
+template <class M, int C_>
+__device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
+                                              const StripCtx &g, FSum &e)
+{
+    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
+        const Site s = make_site(p, g.LP);
+        const Nbrs<typename M::Cell> nb{cells, g.PS, s};
+        M::template energy_site<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
+                                    own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, e);
+    }
+}
+
 // A sample's first half, out of line (it runs once per sample interval and
 // would otherwise crowd the sweep loop's instruction cache): measure the
 // strip, reduce over the CTA, push the partial sums into rank 0's `parts`.
-// The caller arrives at the cluster barrier afterwards, which publishes them.
+// With `epilogue` (a sample on the window's last sweep) the same reduction
+// carries the window epilogue's three sums -- energy change, acceptances,
+// exact energy -- into their slots after the sample's.  The caller arrives
+// at the cluster barrier afterwards, which publishes them.
+template <class M>
+__device__ void window_epilogue_sums(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
+                                     const StripCtx &g, float dsum, float dcomp, int nacc, FSum *v)
+{
+    v[0].hi = dsum;
+    v[0].lo = dcomp;
+    v[1].hi = (float)nacc;  // exact: a thread's count is far below 2^24
+    if (M::kExactEnergy) {
+        energy_colour<M, 0>(ctx, cells, own, g, v[2]);
+        energy_colour<M, 1>(ctx, cells, own, g, v[2]);
+        energy_colour<M, 2>(ctx, cells, own, g, v[2]);
+        energy_colour<M, 3>(ctx, cells, own, g, v[2]);
+    }
+}
+
 template <class M>
 __device__ __noinline__ void push_sample(const typename M::Ctx ctx, typename M::Cell *cells, float *own,
-                                         const StripCtx g, float dsum, float dcomp, float2 *scratch, float2 *parts,
-                                         int rank)
+                                         const StripCtx g, float dsum, float dcomp, int nacc, bool epilogue,
+                                         float2 *scratch, float2 *parts, int rank)
 {
     constexpr int NS = M::kSums;
-    FSum v[NS];
+    FSum v[NS + 3];
     if (M::kEnergyFromDelta) {
         v[0].hi = dsum;
         v[0].lo = dcomp;
@@ -346,11 +376,21 @@ __device__ __noinline__ void push_sample(const typename M::Ctx ctx, typename M::
     measure_colour<M, 1>(ctx, cells, own, g, v);
     measure_colour<M, 2>(ctx, cells, own, g, v);
     measure_colour<M, 3>(ctx, cells, own, g, v);
-    block_fsum<NS>(v, scratch);
-    if (threadIdx.x == 0) {
-        float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * part_slots<M>();
+    float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * part_slots<M>();
+    if (epilogue) {
+        window_epilogue_sums<M>(ctx, cells, own, g, dsum, dcomp, nacc, v + NS);
+        block_fsum<NS + 3>(v, scratch);
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < NS; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
+            for (int q = 0; q < NS + 3; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
+        }
+    } else {
+        FSum (&w)[NS] = *reinterpret_cast<FSum (*)[NS]>(v);
+        block_fsum<NS>(w, scratch);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int q = 0; q < NS; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
+        }
     }
 }
 
@@ -393,17 +433,6 @@ __device__ __noinline__ void combine_sample(const typename M::Ctx ctx, const Win
     __syncwarp();
 }
 
-template <class M, int C_>
-__device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
-                                              const StripCtx &g, FSum &e)
-{
-    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
-        const Site s = make_site(p, g.LP);
-        const Nbrs<typename M::Cell> nb{cells, g.PS, s};
-        M::template energy_site<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
-                                    own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, e);
-    }
-}
 
 // After a cluster's whole work list (thread 0 of its rank-0 CTA): the last
 // cluster to finish advances the device clock by the launch's windows (every
@@ -778,7 +807,6 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                     cluster_arrive();
                     cluster_wait();
                     fused_pass<M, NK, 3>(ctx, cells, own, g, sites, st, dacc, nacc);
-                    cluster_arrive();
                 }
             } else if constexpr (regs) {
                 {
@@ -802,7 +830,6 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 propose_pass<M, NK, 3>(ctx, cells, own, g, sites, st, pa);
                 cluster_wait();
                 decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dacc, nacc);
-                cluster_arrive();
                 }
             } else {
                 (void)sites;
@@ -820,7 +847,6 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 cluster_arrive();
                 cluster_wait();
                 global_rng_pass<M, 3>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
-                cluster_arrive();
             }
 
             comp_add(dsum, dcomp, dacc);
@@ -828,16 +854,25 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 const int slot = next_slot;
                 next_sample += cm.sample_interval;
                 next_slot = next_slot + 1 == cm.n_slots ? 0 : next_slot + 1;
-                // Measure the strip, reduce over the CTA, push the partial
-                // sums into rank 0 ahead of the barrier that ends this phase.
-                cluster_wait();
-                push_sample<M>(ctx, cells, own, g, dsum, dcomp, reinterpret_cast<float2 *>(scratch), parts, rank);
-                pend = (cm.staging != nullptr && s + 1 == cm.n_sweeps) ? -2 : slot;
-                cluster_arrive();
+                // Measure the strip before arriving at the barrier that ends
+                // the sweep.  Once this CTA's own colour-3 moves are done (a
+                // CTA barrier) every cell the measurement reads is final: it
+                // reads the cells below and to the right only, and the one
+                // halo row among them (planes 0/1 below the strip) was last
+                // written in the colour 0-1 phases, published by an earlier
+                // barrier.  Reduce over the CTA, push into rank 0.
+                __syncthreads();
+                const bool last = s + 1 == cm.n_sweeps;
+                push_sample<M>(ctx, cells, own, g, dsum, dcomp, nacc, last, reinterpret_cast<float2 *>(scratch),
+                               parts, rank);
+                pend = (cm.staging != nullptr && last) ? -2 : slot;
             }
+            cluster_arrive();
         }
-        // Ring slot of a sample staged on the window's last sweep (-1: none).
+        // Ring slot of a sample staged on the window's last sweep (-1: none);
+        // a sample on the last sweep has also pushed the epilogue's sums.
         const int end_slot = pend == -2 ? (next_slot == 0 ? cm.n_slots - 1 : next_slot - 1) : -1;
+        const bool epilogue_pushed = pend != -1;
         cluster_wait();
         MCGB_COMBINE_PENDING()
 #undef MCGB_COMBINE_PENDING
@@ -851,22 +886,17 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         long long acc_now = 0;
 
         // Window epilogue: energy and acceptance bookkeeping (compensated
-        // float32 partial sums pushed into rank 0, as for samples), write back.
-        FSum v2[3];
-        v2[0].hi = dsum;
-        v2[0].lo = dcomp;
-        v2[1].hi = (float)nacc;  // exact: a thread's count is far below 2^24
-        if (M::kExactEnergy) {
-            energy_colour<M, 0>(ctx, cells, own, g, v2[2]);
-            energy_colour<M, 1>(ctx, cells, own, g, v2[2]);
-            energy_colour<M, 2>(ctx, cells, own, g, v2[2]);
-            energy_colour<M, 3>(ctx, cells, own, g, v2[2]);
-        }
-        block_fsum<3>(v2, reinterpret_cast<float2 *>(scratch));
-        if (tid == 0) {
-            float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NP + NS;
+        // float32 partial sums pushed into rank 0, as for samples, unless a
+        // sample on the last sweep carried them), write back.
+        if (!epilogue_pushed) {
+            FSum v2[3];
+            window_epilogue_sums<M>(ctx, cells, own, g, dsum, dcomp, nacc, v2);
+            block_fsum<3>(v2, reinterpret_cast<float2 *>(scratch));
+            if (tid == 0) {
+                float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NP + NS;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) dst[q] = make_float2(v2[q].hi, v2[q].lo);
+                for (int q = 0; q < 3; ++q) dst[q] = make_float2(v2[q].hi, v2[q].lo);
+            }
         }
         if (win + 1 == n_windows) {
         for (int c = 0; c < 4; ++c)
@@ -885,7 +915,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
         }
         }
-        cluster.sync();
+        // The epilogue's pushes land before rank 0 merges them: published by
+        // this barrier, or already by the barrier ending the last sweep.
+        if (!epilogue_pushed) cluster.sync();
         if (rank == 0 && tid == 0) {
             FSum de, na, ex;
             for (int k = 0; k < C; ++k) {
