@@ -955,8 +955,13 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             cm.e_run[2 * r + 1] = e_lo;
             cm.accepted[r] = acc_now;
         }
-        __syncwarp();  // the aligned cluster barrier needs warp 0 converged again
-        cluster.sync();
+        __syncwarp();  // the aligned cluster barriers need warp 0 converged again
+        // Between windows of a resident launch every CTA waits for the new
+        // temperature.  After the last window nothing waits: no replica runs
+        // twice in a launch, so the next replica of the work list reads
+        // nothing the exchange writes, and its strip load (cells and halo
+        // rows; the exchange reads neither) overlaps warp 0's exchange.
+        if (win + 1 < n_windows) cluster.sync();
         }  // windows
     }
     if (a.fx.enabled && rank == 0 && tid == 0) launch_finished(a.fx, cm, (int)(gridDim.x / C));
