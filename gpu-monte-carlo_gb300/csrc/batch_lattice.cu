@@ -267,12 +267,15 @@ __global__ void batch_energy64_kernel(int model, const void *state, const mcgb_r
     }
 }
 
+// The (cos, sin) cache from the angles, with the intrinsic the updates use
+// when they store an accepted angle's pair: the cache is a function of the
+// angles alone, so rebuilding it reproduces the evolved cache bit for bit.
 __global__ void refresh_aux_kernel(const float *state, float2 *aux, int64_t n, int stride)
 {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
     float sn, cs;
-    sincosf(state[k * stride], &sn, &cs);
+    __sincosf(state[k * stride], &sn, &cs);
     aux[k] = make_float2(cs, sn);
 }
 

@@ -209,8 +209,9 @@ class LadderBatch:
         self.elem_bytes = self.dtype.itemsize * site
         # The chain state -- spins/angles, RNG streams, running energies and,
         # for XY and Kawamura, the (cos, sin) cache -- lives in one device
-        # allocation (256-byte aligned pieces), so a host round trip is one
-        # copy each way.
+        # allocation (256-byte aligned pieces, the cache last).  The cache is
+        # a function of the angles (refresh_aux reproduces it bit for bit),
+        # so a host round trip moves the prefix before it, one copy each way.
         has_aux = self.model_id in (MODEL_XY, MODEL_KAWAMURA, MODEL_KAWAMURA_GAUSS)
         pieces = [("state", (self.n_sites,) + self.site_shape, self.dtype),
                   ("rng", (self.n_sites,), XOROSHIRO128P_DTYPE),
@@ -226,6 +227,7 @@ class LadderBatch:
         for (name, shape, dt), off in zip(pieces, offsets):
             nb = int(np.prod(shape, dtype=np.int64)) * np.dtype(dt).itemsize
             setattr(self, name, DeviceArray(shape, dt, _storage=self._chain[off:off + max(nb, 1)]))
+        self._chain_host = self._chain[:offsets[3]] if has_aux else self._chain
         if not has_aux:
             self.aux = None
         ref_state = DeviceArray((self.n_sites,) + self.site_shape, self.dtype)
@@ -625,29 +627,30 @@ class LadderBatch:
 
     # ------------------------------------------------------------ host I/O
     def pinned_state_buffers(self):
-        """A pinned host buffer for the whole chain state (spins/angles, RNG
-        streams, running energies, the (cos, sin) cache), engine layout."""
+        """A pinned host buffer for the chain state (spins/angles, RNG
+        streams, running energies), engine layout."""
         import torch as _t
-        return {"chain": _t.empty(self._chain.numel(), dtype=_t.uint8, pin_memory=True)}
+        return {"chain": _t.empty(self._chain_host.numel(), dtype=_t.uint8, pin_memory=True)}
 
     def upload_state(self, host, recompute=False):
         """Asynchronous host-to-device copy from pinned buffers.  A buffer from
         pinned_state_buffers/download_state resumes the chain exactly (one
-        copy); a dict of ``state`` and ``rng`` bytes alone (engine layout)
-        uploads those, then rebuilds the (cos, sin) cache and the exact
-        energies on the device, as does ``recompute``."""
+        copy, then the (cos, sin) cache rebuilt from the angles on the
+        device); a dict of ``state`` and ``rng`` bytes alone (engine layout)
+        uploads those, then also recomputes the exact energies on the
+        device, as does ``recompute``."""
         if "chain" in host:
-            self._chain.copy_(host["chain"], non_blocking=True)
+            self._chain_host.copy_(host["chain"], non_blocking=True)
         else:
             self.state.raw().copy_(host["state"], non_blocking=True)
             self.rng.raw().copy_(host["rng"], non_blocking=True)
+        self.refresh_aux()
         if recompute or "chain" not in host:
-            self.refresh_aux()
             self.recompute_energy()
 
     def download_state(self, host):
         """Asynchronous device-to-host copy of the chain state (one copy)."""
-        host["chain"].copy_(self._chain, non_blocking=True)
+        host["chain"].copy_(self._chain_host, non_blocking=True)
 
     def checkpoint(self):
         """Everything needed to resume the chain bit-exactly, as host arrays."""

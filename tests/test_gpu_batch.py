@@ -388,9 +388,11 @@ def test_simulated_ladders_save_load_and_summarise(tmp_path):
 
 
 def test_host_round_trip_resumes_the_chain_exactly():
-    """download_state/upload_state move the whole chain state (angles, streams,
-    (cos, sin) cache, running energies): resuming from the host copy repeats
-    the same sweeps bit for bit; a state-only upload rebuilds the caches."""
+    """download_state/upload_state move the chain state (angles, streams,
+    running energies; the (cos, sin) cache is rebuilt from the angles on the
+    device, bit for bit what the sweeps left): resuming from the host copy
+    repeats the same sweeps bit for bit; a state-only upload also rebuilds the
+    energies."""
     import torch
     from mcgb.batch import LadderBatch
     from mcgb.models.xy.model import XYModel
@@ -398,8 +400,12 @@ def test_host_round_trip_resumes_the_chain_exactly():
     init = np.random.default_rng(12).uniform(-np.pi, np.pi, (4, L, L)).astype(np.float32)
     b = LadderBatch(XYModel(), [(L, T)], exchange_interval=None, proposal="gaussian", initial_states=[init])
     b.run(30)
+    evolved = b.aux.copy_to_host()
+    b.refresh_aux()
+    np.testing.assert_array_equal(b.aux.copy_to_host().view(np.uint32), evolved.view(np.uint32))
     host = b.pinned_state_buffers()
-    assert set(host) == {"chain"} and host["chain"].numel() >= b.state.nbytes + b.rng.nbytes + b.aux.nbytes
+    assert set(host) == {"chain"} and host["chain"].numel() >= b.state.nbytes + b.rng.nbytes + b.e_run.nbytes
+    assert host["chain"].numel() < b.state.nbytes + b.rng.nbytes + b.aux.nbytes
     b.download_state(host)
     torch.cuda.synchronize()
     b.run(20)
@@ -414,6 +420,20 @@ def test_host_round_trip_resumes_the_chain_exactly():
     b.upload_state({"state": state_bytes, "rng": rng_bytes})
     drift = b.recompute_energy().copy_to_host()
     assert np.all(np.abs(drift) < 1e-6 * L * L)
+
+
+@pytest.mark.parametrize("proposal", ["uniform", "gaussian"])
+def test_kawamura_cache_is_a_function_of_the_angles(proposal):
+    """The Kawamura (cos, sin) cache after sweeps equals its rebuild from the
+    angles bit for bit, so host round trips need not carry it."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.kawamura.model import KawamuraModel
+    b = LadderBatch(KawamuraModel(), [(16, np.geomspace(0.8, 1.2, 4))], exchange_interval=None,
+                    proposal=proposal, cluster_size=2, threads=128)
+    b.run(25)
+    evolved = b.aux.copy_to_host()
+    b.refresh_aux()
+    np.testing.assert_array_equal(b.aux.copy_to_host().view(np.uint32), evolved.view(np.uint32))
 
 
 def test_resident_wait_that_runs_out_is_reported_and_the_batch_recovers():
