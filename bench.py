@@ -381,7 +381,7 @@ def run_mcgb(args, rank, world):
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
     # A resident launch runs a whole step (10 windows with their exchanges);
     # otherwise one fused launch per window.
-    launches = args.steps * (1 if batch.resident else SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
+    launches = args.steps * batch.launches_per_step(SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
 
     line = None
     if rank == 0:
@@ -590,13 +590,15 @@ def run_workload(args, rank, world):
     # The window kernel alone (one window of the schedule, samples on).
     from mcgb.batch import NO_EXCHANGE_WINDOW
     win = ex or NO_EXCHANGE_WINDOW
-    w = batch._window(win)
-    _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+    ws = [batch._window(win, group=g) for g in batch.groups]  # one launch per size group
+    for w in ws:
+        _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
     torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record(stream)
     for _ in range(10):
-        _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+        for w in ws:
+            _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
     k1.record(stream)
     torch.cuda.synchronize()
     window_ms = k0.elapsed_time(k1) / 10
@@ -638,6 +640,8 @@ def run_workload(args, rank, world):
         "config": {"workload": desc, "replicas_per_gpu": int(batch.R), "sites_per_sweep": n_sites,
                    "sweeps_per_step": SWEEPS_PER_STEP, "exchange_interval": ex, "sample_interval": si,
                    "cluster_size": batch.cluster_size, "threads": batch.threads,
+                   "size_groups": [{"L": sizes, "cluster_size": c, "threads": t, "resident": r}
+                                   for sizes, c, t, r in batch.shapes()] if len(batch.groups) > 1 else None,
                    "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": f"independent ladders x{world}"},
         "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
@@ -646,7 +650,7 @@ def run_workload(args, rank, world):
                      "traffic": None, "kernel": f"window_kernel ({kind})", "kernel_ms": window_ms,
                      "bytes_per_update": BYTES[kind], "peak_source": peak_kind},
         "clocks": clk,
-        "gpu_launches": args.steps * (1 if (ex and batch.resident) else windows_per_step * (1 if ex else 2)),
+        "gpu_launches": args.steps * batch.launches_per_step(windows_per_step),
     }
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1

@@ -122,16 +122,26 @@ inline int validate_window(const mcgb_batch_window &w)
     }
     MCGB_REQUIRE(w.samples == nullptr || w.n_temps_total >= w.n_replicas,
                  "batch window: n_temps_total must cover every replica");
+    if (w.host_work_idx != nullptr) {
+        MCGB_REQUIRE(w.n_work >= 1 && w.n_work <= w.n_replicas, "batch window: bad n_work %d", w.n_work);
+        for (int k = 0; k < w.n_work; ++k)
+            MCGB_REQUIRE(w.host_work_idx[k] >= 0 && w.host_work_idx[k] < w.n_replicas,
+                         "batch window: work entry %d names replica %d of %d", k, w.host_work_idx[k], w.n_replicas);
+    }
     return MCGB_OK;
 }
 
-// Shared memory for the largest strip of the batch.
+// The replicas a launch runs: host_work_idx when given, else the table.
+inline int work_count(const mcgb_batch_window &w) { return w.host_work_idx ? w.n_work : w.n_replicas; }
+inline int work_replica(const mcgb_batch_window &w, int k) { return w.host_work_idx ? w.host_work_idx[k] : k; }
+
+// Shared memory for the largest strip among the replicas a launch runs.
 template <class M>
-inline size_t batch_smem(const mcgb_replica *table, int n, int C)
+inline size_t batch_smem(const mcgb_batch_window &w, int C)
 {
     size_t best = 0;
-    for (int r = 0; r < n; ++r) {
-        const int L = table[r].L, Ce = effective_cluster(L, C);
+    for (int k = 0; k < work_count(w); ++k) {
+        const int L = w.host_table[work_replica(w, k)].L, Ce = effective_cluster(L, C);
         const size_t b = window_smem_bytes<M>((long long)L * L / (4 * Ce), (long long)L / 2);
         if (b > best) best = b;
     }
@@ -149,7 +159,7 @@ template <class M, int NPMAX>
 int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t stream, const char *name)
 {
     auto kern = window_kernel<M, NPMAX>;
-    const size_t smem = batch_smem<M>(w.host_table, w.n_replicas, w.cluster_size);
+    const size_t smem = batch_smem<M>(w, w.cluster_size);
     MCGB_REQUIRE(smem <= 232448, "%s: a strip needs %zu bytes of shared memory (> 227 KB); use a larger "
                                  "cluster_size", name, smem);
     int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -196,8 +206,8 @@ template <class M>
 int pick_npmax(const mcgb_batch_window &w)
 {
     long long npl = 0;
-    for (int r = 0; r < w.n_replicas; ++r) {
-        const int L = w.host_table[r].L;
+    for (int k = 0; k < work_count(w); ++k) {
+        const int L = w.host_table[work_replica(w, k)].L;
         const long long n = (long long)L * L / (4 * effective_cluster(L, w.cluster_size));
         if (n > npl) npl = n;
     }

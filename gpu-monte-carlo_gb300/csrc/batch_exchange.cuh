@@ -243,10 +243,12 @@ struct FusedExchange {
     int32_t *error;        // set when a wait for a pair's decision gave up
     int enabled;
     int n_windows;         // > 1: a resident launch (one replica per cluster, cooperative)
+    int hold_clock;        // another launch of the same windows advances the clock
     long long wait_limit;  // polls of a pair's decision before a wait gives up
 };
 
-inline FusedExchange make_fused(const ExchangeArgs &ex, int32_t *sync, int n_windows, long long wait_limit)
+inline FusedExchange make_fused(const ExchangeArgs &ex, int32_t *sync, int n_windows, int hold_clock,
+                                long long wait_limit)
 {
     const int n = ex.n_replicas;
     FusedExchange fx;
@@ -257,6 +259,7 @@ inline FusedExchange make_fused(const ExchangeArgs &ex, int32_t *sync, int n_win
     fx.error = sync + 5ll * n + 1;
     fx.enabled = 1;
     fx.n_windows = n_windows;
+    fx.hold_clock = hold_clock;
     fx.wait_limit = wait_limit;
     return fx;
 }

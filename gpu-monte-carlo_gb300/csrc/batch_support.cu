@@ -167,7 +167,7 @@ extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w,
     if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
     MCGB_REQUIRE((reinterpret_cast<uintptr_t>(sync) & 15) == 0, "window_exchange: sync must be 16-byte aligned");
     MCGB_REQUIRE(pt->channels <= 32, "window_exchange: at most 32 sample channels");
-    const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, 1, kWaitSpinLimit);
+    const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, 1, w->hold_clock, kWaitSpinLimit);
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
 }
@@ -188,15 +188,15 @@ extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, co
     MCGB_REQUIRE(w && pt, "run_resident: null argument block");
     MCGB_REQUIRE(sync != nullptr, "run_resident: null sync counters");
     MCGB_REQUIRE(n_windows >= 1, "run_resident: n_windows must be >= 1");
-    MCGB_REQUIRE(n_windows == 1 || w->n_clusters == w->n_replicas,
-                 "run_resident: a resident launch needs one cluster per replica (n_clusters == n_replicas)");
+    MCGB_REQUIRE(n_windows == 1 || w->n_clusters == work_count(*w),
+                 "run_resident: a resident launch needs one cluster per replica it runs");
     if (int st = check_exchange(*w, *pt)) return st;
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w->J > 0, "XY: J must be positive");
     if (model == MCGB_MODEL_HE3_GAUSS) MCGB_REQUIRE(w->counters != nullptr, "He3 Gaussian: null counters");
     if (model == MCGB_MODEL_KAWAMURA_GAUSS) MCGB_REQUIRE(w->sigma_t != nullptr, "Kawamura Gaussian: null widths");
     MCGB_REQUIRE((reinterpret_cast<uintptr_t>(sync) & 15) == 0, "run_resident: sync must be 16-byte aligned");
     MCGB_REQUIRE(pt->channels <= 32, "run_resident: at most 32 sample channels");
-    const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, n_windows, g_wait_limit);
+    const FusedExchange fx = make_fused(make_exchange_args(*w, *pt), sync, n_windows, w->hold_clock, g_wait_limit);
     return is_lattice(model) ? lattice_window(model, *w, as_stream(stream), &fx)
                              : continuum_window(model, *w, as_stream(stream), &fx);
 }

@@ -436,15 +436,18 @@ __device__ __noinline__ void combine_sample(const typename M::Ctx ctx, const Win
 
 // After a cluster's whole work list (thread 0 of its rank-0 CTA): the last
 // cluster to finish advances the device clock by the launch's windows (every
-// cluster has read it at its start) and resets the launch counter.
+// cluster has read it at its start; unless another launch of the same
+// windows does) and resets the launch counter.
 __device__ __forceinline__ void launch_finished(const FusedExchange &fx, const WindowCommon &cm, int n_clusters)
 {
     __threadfence();
     if (atomicAdd(fx.launch_done, 1) == n_clusters - 1) {
         __threadfence();
-        long long *clock = const_cast<long long *>(cm.clock);
-        clock[0] = __ldcg(clock) + (long long)cm.n_sweeps * fx.n_windows;
-        clock[1] = __ldcg(clock + 1) + fx.n_windows;
+        if (!fx.hold_clock) {
+            long long *clock = const_cast<long long *>(cm.clock);
+            clock[0] = __ldcg(clock) + (long long)cm.n_sweeps * fx.n_windows;
+            clock[1] = __ldcg(clock + 1) + fx.n_windows;
+        }
         *fx.launch_done = 0;
         __threadfence();
     }

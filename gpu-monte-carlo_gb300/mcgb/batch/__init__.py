@@ -69,6 +69,7 @@ class BatchWindow(ctypes.Structure):
         ("J", ctypes.c_float), ("delta", ctypes.c_float), ("sigma_t", ctypes.c_void_p),
         ("coefficients", ctypes.c_float * 5), ("K", ctypes.c_float), ("g_d", ctypes.c_float),
         ("rho", ctypes.c_float), ("mass", ctypes.c_float),
+        ("host_work_idx", ctypes.c_void_p), ("n_work", ctypes.c_int32), ("hold_clock", ctypes.c_int32),
     ]
 
 
@@ -115,6 +116,18 @@ def lpt_work_lists(costs, n_clusters):
     for k, x in enumerate(lists):
         loads[k] = sum(costs[r] for r in x)
     return ptrs, idx, loads
+
+
+class _Group:
+    """Replicas that share one cluster shape: one launch per window (or one
+    resident launch of many windows) runs them.  A ladder has one lattice
+    size, so grouping by size never splits a ladder."""
+
+    def __init__(self, idx):
+        self.idx = np.asarray(idx, dtype=np.int64)
+        self.cluster_size = self.threads = self.n_clusters = 0
+        self.work_ptr = self.work_idx = self.work_host = None
+        self.resident = False
 
 
 def _validate_ladder(L, temperatures, pt):
@@ -299,6 +312,7 @@ class LadderBatch:
         self.first_sample_sweep = 0
         self.sample_interval = 0
         self._graphs = {}
+        self.groups = [_Group(np.arange(self.R))]
         self.configure(cluster_size, threads)
         self.refresh_aux()
         self.recompute_energy()
@@ -343,9 +357,12 @@ class LadderBatch:
         return np.stack([h["s0"], h["s1"]], axis=1)
 
     # ------------------------------------------------------------ launch shape
-    def _smem(self, C):
+    def _sizes(self, idx=None):
+        return np.unique(self.table_host["L"] if idx is None else self.table_host["L"][idx])
+
+    def _smem(self, C, idx=None):
         best = 0
-        for L in np.unique(self.table_host["L"]):
+        for L in self._sizes(idx):
             v = int(_lib.load().mcgb_batch_smem_bytes(self.model_id, int(L), int(C)))
             if v < 0:
                 _lib.check(v, "mcgb_batch_smem_bytes")
@@ -361,15 +378,16 @@ class LadderBatch:
                 return c
         return 1
 
-    def candidate_shapes(self):
-        """(cluster_size, threads) pairs valid for every replica of the batch."""
+    def candidate_shapes(self, idx=None):
+        """(cluster_size, threads) pairs valid for every replica of the batch
+        (or of the replicas `idx`)."""
         out = []
-        Ls = self.table_host["L"]
+        Ls = self._sizes(idx)
         for C in (1, 2, 4, 8, 16):
-            smem = self._smem(C)
+            smem = self._smem(C, idx)
             if smem > 232448:
                 continue
-            npl_max = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in np.unique(Ls))
+            npl_max = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in Ls)
             t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512,
                      MODEL_KAWAMURA_GAUSS: 512}.get(self.model_id, 1024)
             for T in (128, 256, 512, 1024):
@@ -378,33 +396,41 @@ class LadderBatch:
                 out.append((C, T))
         return out
 
-    def _costs(self, C):
+    def _costs(self, C, idx=None):
         """Relative time a cluster spends on each replica (sites per active CTA)."""
-        Ls = self.table_host["L"].astype(np.int64)
+        Ls = (self.table_host["L"] if idx is None else self.table_host["L"][idx]).astype(np.int64)
         return np.array([L * L / self.effective_cluster(L, C) for L in Ls], dtype=np.float64)
 
-    def max_clusters(self, C, T):
+    def max_clusters(self, C, T, idx=None):
         n = ctypes.c_int(0)
-        _lib.call("mcgb_batch_max_clusters", self.model_id, C, T, self._smem(C), ctypes.byref(n))
+        _lib.call("mcgb_batch_max_clusters", self.model_id, C, T, self._smem(C, idx), ctypes.byref(n))
         return n.value
 
     def configure(self, cluster_size=None, threads=None):
-        """Choose the cluster shape (heuristic unless given) and build work lists."""
+        """Choose each group's cluster shape (heuristic unless given) and build
+        its work lists."""
+        for g in self.groups:
+            self._configure_group(g, cluster_size, threads)
+        self._resident_checked = False
+        self._graphs.clear()
+
+    def _configure_group(self, g, cluster_size=None, threads=None):
+        idx = g.idx
         if cluster_size is None or threads is None:
             best = None
-            for C, T in self.candidate_shapes():
+            Ls = self._sizes(idx)
+            for C, T in self.candidate_shapes(idx):
                 if cluster_size is not None and C != cluster_size:
                     continue
                 if threads is not None and T != threads:
                     continue
-                m = self.max_clusters(C, T)
+                m = self.max_clusters(C, T, idx)
                 if m < 1:
                     continue
-                ncl = min(m, self.R)
+                ncl = min(m, len(idx))
                 # Estimated window time ~ (largest cluster load) / threads.
-                costs = self._costs(C)
-                _, _, loads = lpt_work_lists(costs, ncl)
-                npl = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in np.unique(self.table_host["L"]))
+                _, _, loads = lpt_work_lists(self._costs(C, idx), ncl)
+                npl = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in Ls)
                 occupancy = min(1.0, npl / T)
                 score = loads.max() / (T * occupancy) + 0.02 * C
                 if best is None or score < best[0]:
@@ -412,32 +438,83 @@ class LadderBatch:
             if best is None:
                 raise ValueError("no cluster shape fits this batch")
             _, cluster_size, threads = best
-        if int(cluster_size) not in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16):
+        if int(cluster_size) not in range(1, 17):
             raise ValueError("cluster_size must be 1..16")
-        if self._smem(int(cluster_size)) > 232448:
+        if self._smem(int(cluster_size), idx) > 232448:
             raise ValueError("a strip does not fit in shared memory; use a larger cluster_size")
-        self.cluster_size, self.threads = int(cluster_size), int(threads)
-        m = self.max_clusters(self.cluster_size, self.threads)
+        C, T = int(cluster_size), int(threads)
+        m = self.max_clusters(C, T, idx)
         if m < 1:
-            raise ValueError(f"cluster shape ({cluster_size}, {threads}) cannot be resident")
-        self.n_clusters = min(m, self.R)
-        wp, wi, _ = lpt_work_lists(self._costs(self.cluster_size), self.n_clusters)
-        self.work_ptr, self.work_idx = to_device(wp), to_device(wi)
+            raise ValueError(f"cluster shape ({C}, {T}) cannot be resident")
+        g.cluster_size, g.threads, g.n_clusters = C, T, min(m, len(idx))
+        wp, wi, _ = lpt_work_lists(self._costs(C, idx), g.n_clusters)
+        g.work_host = np.ascontiguousarray(idx[wi].astype(np.int32))
+        g.work_ptr, g.work_idx = to_device(wp), to_device(g.work_host)
         # Resident launches (many windows per launch, strips kept on chip)
         # need one replica per cluster and every cluster resident at once.
-        self.resident = (self._resident_wanted and self.pt and self.n_clusters == self.R
-                         and bool(np.all(np.diff(wp) == 1)))
-        self._resident_checked = False
-        self._graphs.clear()
+        g.resident = (self._resident_wanted and self.pt and g.n_clusters == len(idx)
+                      and bool(np.all(np.diff(wp) == 1)))
+
+    def split_by_size(self, split=True):
+        """One group -- one launch per window, its own cluster shape -- per
+        lattice size (split=True), or one group for the whole batch."""
+        Ls = self.table_host["L"]
+        if split:
+            self.groups = [_Group(np.flatnonzero(Ls == L)) for L in np.unique(Ls)]
+        else:
+            self.groups = [_Group(np.arange(self.R))]
+        self.configure()
+
+    # The first group's shape (the only group unless the batch is split).
+    @property
+    def cluster_size(self):
+        return self.groups[0].cluster_size
+
+    @property
+    def threads(self):
+        return self.groups[0].threads
+
+    @property
+    def n_clusters(self):
+        return self.groups[0].n_clusters
+
+    @property
+    def work_ptr(self):
+        return self.groups[0].work_ptr
+
+    @property
+    def work_idx(self):
+        return self.groups[0].work_idx
+
+    @property
+    def resident(self):
+        """Whether exchange windows run as resident launches (any group)."""
+        return any(g.resident for g in self.groups)
+
+    def launches_per_step(self, n_windows):
+        """Kernel launches of a step of n_windows full windows: per group one
+        resident launch or one fused launch per window with exchange; without
+        exchange, per window one launch per group and the clock tick."""
+        if self.pt:
+            return sum(1 if (g.resident and n_windows > 1) else n_windows for g in self.groups)
+        return n_windows * (len(self.groups) + 1)
+
+    def shapes(self):
+        """[(lattice sizes, cluster_size, threads, resident)] per group."""
+        return [([int(L) for L in self._sizes(g.idx)], g.cluster_size, g.threads, g.resident) for g in self.groups]
 
     # ------------------------------------------------------------ argument blocks
-    def _window(self, n_sweeps, staging=False):
+    def _window(self, n_sweeps, staging=False, group=None):
+        g = self.groups[0] if group is None else group
         w = BatchWindow()
         w.table = self.table.ptr
         w.host_table = self.table_host.ctypes.data
         w.n_replicas = self.R
-        w.work_ptr, w.work_idx = self.work_ptr.ptr, self.work_idx.ptr
-        w.n_clusters, w.cluster_size, w.threads = self.n_clusters, self.cluster_size, self.threads
+        w.work_ptr, w.work_idx = g.work_ptr.ptr, g.work_idx.ptr
+        w.n_clusters, w.cluster_size, w.threads = g.n_clusters, g.cluster_size, g.threads
+        if len(self.groups) > 1:
+            w.host_work_idx = g.work_host.ctypes.data
+            w.n_work = len(g.idx)
         w.state, w.rng, w.betas, w.w2t = self.state.ptr, self.rng.ptr, self.betas.ptr, self.w2t.ptr
         w.aux = None if self.aux is None else self.aux.ptr
         w.e_run, w.energies, w.accepted = self.e_run.ptr, self.energies.ptr, self.accepted.ptr
@@ -474,16 +551,22 @@ class LadderBatch:
     # ------------------------------------------------------------ stepping
     def _enqueue_window(self, n_sweeps, exchange, tune=False):
         s = _lib.stream_handle()
-        w = self._window(n_sweeps, staging=exchange)
-        self._keep = w
         if exchange and not tune:
-            # Window, per-ladder exchanges and clock tick in one launch.
+            # Window, exchange and clock tick in one launch per group (the
+            # last group's launch advances the clock).
             p = self._pt()
             self._keep_pt = p
-            _lib.call("mcgb_batch_window_exchange", self.model_id, ctypes.byref(w), ctypes.byref(p),
-                      self.sync.cptr, s)
+            for i, g in enumerate(self.groups):
+                w = self._window(n_sweeps, staging=True, group=g)
+                w.hold_clock = int(i + 1 < len(self.groups))
+                self._keep = w
+                _lib.call("mcgb_batch_window_exchange", self.model_id, ctypes.byref(w), ctypes.byref(p),
+                          self.sync.cptr, s)
             return
-        _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
+        for g in self.groups:
+            w = self._window(n_sweeps, staging=exchange, group=g)
+            self._keep = w
+            _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
         if tune:
             # The window's acceptance belongs to the temperatures it ran at:
             # tune before the exchange moves replicas.
@@ -544,27 +627,50 @@ class LadderBatch:
         if exchanged:
             self.exchange_rounds += times
 
-    def _enqueue_resident(self, n_sweeps, count):
+    def _enqueue_resident(self, n_sweeps, count, fallback=False):
+        """`count` exchange windows: one resident launch per resident group,
+        then, window by window, one launch per other group.  Every launch
+        reads the clock as the step found it but the one that advances it:
+        the last launch of a window (or the last resident launch when every
+        group is resident).  With `fallback`, a group whose cooperative launch
+        is refused (nothing of it runs) moves to the window-by-window launches."""
         s = _lib.stream_handle()
-        w = self._window(n_sweeps, staging=True)
         p = self._pt()
-        self._keep, self._keep_pt = w, p
-        _lib.call("mcgb_batch_run_resident", self.model_id, ctypes.byref(w), ctypes.byref(p), self.sync.cptr,
-                  int(count), s)
+        self._keep_pt = p
+        res = [g for g in self.groups if g.resident]
+        non = [g for g in self.groups if not g.resident]
+        for i, g in enumerate(res):
+            w = self._window(n_sweeps, staging=True, group=g)
+            w.hold_clock = int(bool(non) or i + 1 < len(res))
+            self._keep = w
+            try:
+                _lib.call("mcgb_batch_run_resident", self.model_id, ctypes.byref(w), ctypes.byref(p),
+                          self.sync.cptr, int(count), s)
+            except _lib.MCGBError:
+                if not fallback:
+                    raise
+                g.resident = False
+                non.append(g)
+        for _ in range(count if non else 0):
+            for i, g in enumerate(non):
+                w = self._window(n_sweeps, staging=True, group=g)
+                w.hold_clock = int(i + 1 < len(non))
+                self._keep = w
+                _lib.call("mcgb_batch_window_exchange", self.model_id, ctypes.byref(w), ctypes.byref(p),
+                          self.sync.cptr, s)
 
     def _replay(self, count, step, tune):
         resident = self.resident and step[1] and not tune and count > 1
         if resident and not self._resident_checked:
-            # First resident launch runs directly: if this device cannot hold
-            # every cluster at once the cooperative launch fails before doing
-            # anything, and the batch falls back to one launch per window.
-            try:
-                self._enqueue_resident(step[0], count)
-                self._resident_checked = True
-                self._advance(step[0], step[1], count)
-                return
-            except _lib.MCGBError:
-                self.resident, resident = False, False
+            # The first resident step runs directly: a group whose clusters
+            # cannot all be resident on this device has its cooperative launch
+            # refused before anything of it runs, and falls back to one
+            # launch per window.
+            self._enqueue_resident(step[0], count, fallback=True)
+            self._resident_checked = True
+            self._graphs.clear()
+            self._advance(step[0], step[1], count)
+            return
         key = (count, step, tune, self.samples is not None and self.samples.ptr, resident)
         g = self._graphs.get(key)
         if g is None:
@@ -786,11 +892,14 @@ class LadderBatch:
         }
 
     # ------------------------------------------------------------ autotuning
-    def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False):
+    def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False, split=None):
         """Time each valid (cluster_size, threads) on a copy-free trial window
-        and keep the fastest.  State and RNG are saved and restored, so tuning
-        does not change the Markov chain."""
-        shapes = shapes or self.candidate_shapes()
+        and keep the fastest, per group.  For a batch of several lattice sizes
+        (`split` None) it also times one group per size and keeps that when
+        its summed window time beats the best single launch by 5 %; `split`
+        True/False forces either.  State and RNG are saved and restored, so
+        tuning does not change the Markov chain.  Returns the trial times
+        [(ms, cluster_size, threads)] of the kept grouping's groups."""
         n = sweeps_per_trial or (self.exchange_interval or 10)
         saved_state = self.state.raw().clone()
         saved_aux = None if self.aux is None else self.aux.raw().clone()
@@ -799,14 +908,57 @@ class LadderBatch:
         saved_acc = self.accepted.raw().clone()
         saved_clock = self.clock.raw().clone()
         saved_samples, self.samples = self.samples, None
+
+        def tune_groups():
+            total, trials = 0.0, []
+            for g in self.groups:
+                res = self._tune_group(g, n, shapes, verbose)
+                total += res[0][0]
+                trials += res
+            return total, trials
+
+        ragged = len(self._sizes()) > 1
+        if split is None and ragged:
+            self.split_by_size(False)
+            one, one_trials = tune_groups()
+            one_shape = (self.cluster_size, self.threads)
+            self.split_by_size(True)
+            many, many_trials = tune_groups()
+            if verbose:
+                print(f"autotune: one launch {one:.3f} ms, one per size {many:.3f} ms per {n}-sweep window")
+            if many < 0.95 * one:
+                results = many_trials
+            else:
+                self.split_by_size(False)
+                self.configure(*one_shape)
+                results = one_trials
+        else:
+            if split is not None and ragged and split != (len(self.groups) > 1):
+                self.split_by_size(split)
+            _, results = tune_groups()
+        self.state.raw().copy_(saved_state)
+        if saved_aux is not None:
+            self.aux.raw().copy_(saved_aux)
+        self.rng.raw().copy_(saved_rng)
+        self.e_run.raw().copy_(saved_e)
+        self.accepted.raw().copy_(saved_acc)
+        self.clock.raw().copy_(saved_clock)
+        self.samples = saved_samples
+        self._graphs.clear()
+        self._resident_checked = False
+        self.recompute_energy()
+        return results
+
+    def _tune_group(self, g, n, shapes=None, verbose=False):
+        """Time group g's window over its candidate shapes; keep the fastest."""
         results = []
-        for C, T in shapes:
+        for C, T in (shapes or self.candidate_shapes(g.idx)):
             try:
-                self.configure(C, T)
+                self._configure_group(g, C, T)
             except ValueError:
                 continue
             s = _lib.stream_handle()
-            w = self._window(n)
+            w = self._window(n, group=g)
             _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
             torch.cuda.synchronize()
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -819,19 +971,12 @@ class LadderBatch:
             ms = ev0.elapsed_time(ev1) / reps
             results.append((ms, C, T))
             if verbose:
-                print(f"autotune C={C} T={T}: {ms:.3f} ms per {n}-sweep window")
-        self.state.raw().copy_(saved_state)
-        if saved_aux is not None:
-            self.aux.raw().copy_(saved_aux)
-        self.rng.raw().copy_(saved_rng)
-        self.e_run.raw().copy_(saved_e)
-        self.accepted.raw().copy_(saved_acc)
-        self.clock.raw().copy_(saved_clock)
-        self.samples = saved_samples
+                print(f"autotune sizes {list(self._sizes(g.idx))} C={C} T={T}: {ms:.3f} ms per {n}-sweep window")
+        if not results:
+            raise ValueError("no cluster shape fits this group")
         results.sort()
         _, C, T = results[0]
-        self.configure(C, T)
-        self.recompute_energy()
+        self._configure_group(g, C, T)
         return results
 
 

@@ -232,6 +232,14 @@ typedef struct mcgb_batch_window {
     float J, delta;                 /* Ising/XY/Kawamura coupling, uniform proposal width */
     const float *sigma_t;           /* XY: Gaussian width per temperature slot (NULL = uniform delta) */
     float coefficients[5], K, g_d, rho, mass; /* He3 */
+    const int32_t *host_work_idx;   /* host copy of work_idx (n_work entries), or NULL: the work
+                                       lists hold every replica of the table; a launch over part of
+                                       the table (one size group) sizes shared memory and picks its
+                                       variant from the replicas listed here */
+    int32_t n_work;                 /* entries in host_work_idx */
+    int32_t hold_clock;             /* fused window + exchange launches: nonzero leaves the clock to
+                                       another launch of the same window (several size groups each
+                                       run the window over their replicas; the last one advances) */
 } mcgb_batch_window;
 
 /* Number of float64 sample channels a model writes per replica. */
