@@ -5,10 +5,14 @@ launches per sweep, an energy reduction and an exchange kernel every
 ``exchange_interval`` sweeps and a measurement kernel plus a host copy per
 sample (core/runtime.py:87-99, core/parallel_tempering.py:245-273,
 core/simulation.py:28-96).  :class:`LadderBatch` runs the same schedule for a
-table of replicas of any mix of L: one cluster-per-replica window kernel of
-``exchange_interval`` sweeps (state in shared memory, RNG in registers), one
-exchange kernel over all ladders and a clock tick, captured as a CUDA graph
-and replayed; samples accumulate in a device buffer that is copied once.
+table of replicas of any mix of L: one launch per window of
+``exchange_interval`` sweeps (a thread-block cluster per replica, state in
+shared memory, RNG in registers) that also decides the replica exchange pair
+by pair and ticks the clock -- or one resident launch of many such windows
+-- captured as a CUDA graph and replayed; samples accumulate in a device
+buffer that is copied once.  A batch of several sizes may run one launch per
+size group, each with its own cluster shape (:meth:`LadderBatch.split_by_size`,
+chosen by :meth:`LadderBatch.autotune` when faster).
 
 Replica (L, ladder k, slot t) keeps the RNG stream that a ``Runtime`` of that
 ladder with seed ``seeds[k]`` gives the same site, so an Ising batch is

@@ -78,10 +78,10 @@ int mcgb_ising_measure(const int8_t *spins, int R, int L, float J,
 int mcgb_xy_update_color(float *theta, void *rng, const float *betas, int R, int L, int color,
                          float J, float delta, void *stream);
 /* Gaussian proposal theta + sigma_r * z (per-walker sigma), same acceptance
- * rule; two draws per visit (the Box-Muller pair from bits 63..41 and 40..18
- * of the first, the acceptance uniform from the second).  No reference
- * counterpart (configuration option "Gaussian MH proposals"); oracle:
- * orc_xy_update_color_gauss. */
+ * rule; one draw per visit: u1 = (2k+1) 2^-22 from bits 63..43, u2 = k 2^-21
+ * from bits 42..22 (the Box-Muller pair) and the acceptance uniform
+ * k 2^-21 from bits 21..1.  No reference counterpart (configuration option
+ * "Gaussian MH proposals"); oracle: orc_xy_update_color_gauss. */
 int mcgb_xy_update_color_gauss(float *theta, void *rng, const float *betas,
                                const float *sigmas, int R, int L, int color, float J,
                                void *stream);
