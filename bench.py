@@ -201,7 +201,9 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     cores = os.cpu_count() or 1
-    sweeps = SWEEPS_PER_STEP
+    # A bounded sample of the workload per step (two exchange windows, about
+    # 0.1 s on 16 cores), so K steps end within minutes for any usual K.
+    sweeps = 2 * EXCHANGE_INTERVAL
     cpu_sample(cores, 10)  # warm-up pages and threads
     vals = []
     t_start = time.perf_counter()
@@ -218,7 +220,8 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform angles)",
-        "config": {"workload": WORKLOAD, "sweeps_per_step": sweeps, "parallelism": "host threads"},
+        "config": {"workload": WORKLOAD, "sweeps_per_step": sweeps, "parallelism": "host threads",
+                   "step": f"a bounded sample: {sweeps} of the workload's {SWEEPS_PER_STEP} sweeps per step"},
         "cpu_baseline": {"value": value, "unit": "updates/ns", "cores": cores, "kind": "port",
                          "sample": f"{sweeps} sweeps of the 32-replica L=128 ladder per step, exchange "
                                    f"every 10 sweeps, {cores} OpenMP threads (the reference has no CPU "
