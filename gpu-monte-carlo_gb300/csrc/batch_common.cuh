@@ -76,33 +76,68 @@ struct FSum {
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
-// Block reduction of NS compensated sums, all on the FP32 pipe; the result is
-// valid in thread 0.  `scratch` holds 32 * NS float2.
-template <int NS>
-__device__ __forceinline__ void block_fsum(FSum (&v)[NS], float2 *scratch)
+// Warp reduce-scatter of P compensated sums (P a power of two <= 32): each of
+// the first log2(P) shuffle levels halves the values a lane carries (the
+// lane whose offset bit is set keeps the upper half and sends the lower),
+// plain butterfly levels finish.  Lane l ends with the warp total of value
+// l >> (5 - log2 P), in every lane of its group.  18 shuffles for 8 sums
+// where one butterfly per sum takes 80.
+template <int P>
+__device__ __forceinline__ void warp_reduce_scatter(FSum (&u)[P], int lane)
 {
+    static_assert(P >= 1 && P <= 32 && (P & (P - 1)) == 0, "P must be a power of two <= 32");
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int half = P / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < half; ++k) {
+            FSum keep = up ? u[k + half] : u[k];
+            const FSum send = up ? u[k] : u[k + half];
+            keep.merge(__shfl_xor_sync(full, send.hi, o), __shfl_xor_sync(full, send.lo, o));
+            u[k] = keep;
+        }
+    }
+#pragma unroll
+    for (int o = 16 / P; o >= 1; o >>= 1) u[0].merge(__shfl_xor_sync(full, u[0].hi, o), __shfl_xor_sync(full, u[0].lo, o));
+}
+
+template <int N>
+struct Pow2Ceil {
+    static constexpr int value = N <= 1 ? 1 : 2 * Pow2Ceil<(N + 1) / 2>::value;
+};
+template <>
+struct Pow2Ceil<1> {
+    static constexpr int value = 1;
+};
+
+// Block reduction of N compensated sums (N <= 32) by warp reduce-scatters,
+// the totals written to dst[0..N) by the lanes of warp 0 that hold them (a
+// DSMEM address works).  `scratch` holds 32 * N float2.  All threads call;
+// the same threads, values and order give the same bits every time.
+template <int N>
+__device__ __forceinline__ void block_fsum_push(const FSum (&v)[N], float2 *scratch, float2 *dst)
+{
+    constexpr int P = Pow2Ceil<N>::value;
+    constexpr int shift = P == 1 ? 5 : (P == 2 ? 4 : (P == 4 ? 3 : (P == 8 ? 2 : (P == 16 ? 1 : 0))));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
+    FSum u[P];
 #pragma unroll
-    for (int q = 0; q < NS; ++q)
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
-            v[q].merge(__shfl_xor_sync(0xffffffffu, v[q].hi, off), __shfl_xor_sync(0xffffffffu, v[q].lo, off));
-    if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < NS; ++q) scratch[q * 32 + warp] = make_float2(v[q].hi, v[q].lo);
-    }
+    for (int q = 0; q < N; ++q) u[q] = v[q];
+    warp_reduce_scatter<P>(u, lane);
+    const int j = lane >> shift;
+    if ((lane & ((1 << shift) - 1)) == 0 && j < N) scratch[j * 32 + warp] = make_float2(u[0].hi, u[0].lo);
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
-        for (int q = 0; q < NS; ++q) {
-            const float2 x = lane < nwarps ? scratch[q * 32 + lane] : make_float2(0.0f, 0.0f);
-            v[q].hi = x.x;
-            v[q].lo = x.y;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1)
-                v[q].merge(__shfl_xor_sync(0xffffffffu, v[q].hi, off), __shfl_xor_sync(0xffffffffu, v[q].lo, off));
+        for (int q = 0; q < P; ++q) {
+            const float2 x = (q < N && lane < nwarps) ? scratch[q * 32 + lane] : make_float2(0.0f, 0.0f);
+            u[q].hi = x.x;
+            u[q].lo = x.y;
         }
+        warp_reduce_scatter<P>(u, lane);
+        if ((lane & ((1 << shift) - 1)) == 0 && j < N) dst[j] = make_float2(u[0].hi, u[0].lo);
     }
 }
 

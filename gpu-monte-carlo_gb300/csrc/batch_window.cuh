@@ -379,18 +379,10 @@ __device__ __noinline__ void push_sample(const typename M::Ctx ctx, typename M::
     float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * part_slots<M>();
     if (epilogue) {
         window_epilogue_sums<M>(ctx, cells, own, g, dsum, dcomp, nacc, v + NS);
-        block_fsum<NS + 3>(v, scratch);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int q = 0; q < NS + 3; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
-        }
+        block_fsum_push<NS + 3>(v, scratch, dst);
     } else {
-        FSum (&w)[NS] = *reinterpret_cast<FSum (*)[NS]>(v);
-        block_fsum<NS>(w, scratch);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int q = 0; q < NS; ++q) dst[q] = make_float2(v[q].hi, v[q].lo);
-        }
+        const FSum (&w)[NS] = *reinterpret_cast<const FSum (*)[NS]>(v);
+        block_fsum_push<NS>(w, scratch, dst);
     }
 }
 
@@ -894,12 +886,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         if (!epilogue_pushed) {
             FSum v2[3];
             window_epilogue_sums<M>(ctx, cells, own, g, dsum, dcomp, nacc, v2);
-            block_fsum<3>(v2, reinterpret_cast<float2 *>(scratch));
-            if (tid == 0) {
-                float2 *dst = static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NP + NS;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) dst[q] = make_float2(v2[q].hi, v2[q].lo);
-            }
+            block_fsum_push<3>(v2, reinterpret_cast<float2 *>(scratch),
+                               static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NP + NS);
         }
         if (win + 1 == n_windows) {
         for (int c = 0; c < 4; ++c)
