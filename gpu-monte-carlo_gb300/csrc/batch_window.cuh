@@ -15,8 +15,9 @@
 // rank 0's shared memory before the barrier that ends the sweep; one warp of
 // rank 0 combines the partial sums after the next wait and writes the sample
 // in temperature order (or stages it for the exchange when it falls on the
-// window's last sweep).  With a FusedExchange the same launch also runs each
-// ladder's replica exchange and advances the device clock.
+// window's last sweep).  With a FusedExchange the same launch also runs the
+// replica exchange, pair by pair as both walkers of a pair finish
+// (pair_finished), and advances the device clock.
 //
 // Halo rows.  Each colour plane of a strip is stored with one halo row above
 // and one below, so every neighbour read is a local shared-memory load at a
