@@ -45,8 +45,10 @@ def test_ising_batch_bit_exact_with_dropin_runtime(cluster_size, threads):
         np.testing.assert_array_equal(e[k], oracle.ising_energy(b.ladder_state(k), np.float32(1))[0])
 
 
-def test_ising_batch_pt_simulation_equals_dropin_simulation():
-    """Same seeds: identical samples, maps and swap counters to Simulation(ParallelTempering)."""
+@pytest.mark.parametrize("L2,split", [(16, False), (24, True)])
+def test_ising_batch_pt_simulation_equals_dropin_simulation(L2, split):
+    """Same seeds: identical samples, maps and swap counters to Simulation(ParallelTempering),
+    also with the ladders of two sizes run as one launch per size."""
     from mcgb.batch import LadderBatch
     from mcgb.core.parallel_tempering import ParallelTempering
     from mcgb.core.runtime import Runtime
@@ -54,12 +56,16 @@ def test_ising_batch_pt_simulation_equals_dropin_simulation():
     from mcgb.models.ising.model import IsingModel
     L, temps = 16, np.geomspace(1.8, 3.0, 5)
     init = seeded_spins(np.random.default_rng(5), 5, L)
-    b = LadderBatch(IsingModel(), [(L, temps), (16, temps[:4])], seeds=[58, 77], exchange_interval=3,
+    init2 = seeded_spins(np.random.default_rng(6), 4, L2)
+    b = LadderBatch(IsingModel(), [(L, temps), (L2, temps[:4])], seeds=[58, 77], exchange_interval=3,
                     exchange_seeds=[59, 78], cluster_size=2, threads=128,
-                    initial_states=[init, init[:4].copy()])
+                    initial_states=[init, init2])
+    if split:
+        b.split_by_size(True)
+        assert len(b.groups) == 2
     runs = b.simulate(thermalization_sweeps=7, measurement_sweeps=40, sample_interval=2)
-    for k, (init_k, T_k, seed) in enumerate(((init, temps, 58), (init[:4].copy(), temps[:4], 77))):
-        rt = Runtime(IsingModel(), L, T_k, seed=seed)
+    for k, (Lk, init_k, T_k, seed) in enumerate(((L, init, temps, 58), (L2, init2, temps[:4], 77))):
+        rt = Runtime(IsingModel(), Lk, T_k, seed=seed)
         rt.state.copy_to_device(init_k)
         pt = ParallelTempering(rt, exchange_interval=3, seed=seed + 1)
         ref = Simulation(pt, thermalization_sweeps=7, measurement_sweeps=40, sample_interval=2).run()
