@@ -201,7 +201,9 @@ int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s
 // The variant a batch runs: the streams in registers when every strip fits,
 // preferring the two-plaquette variant (compiled for fewer threads, so with
 // the larger register budget) whenever the thread count allows it; else the
-// global-memory streams variant (NPMAX = 0).
+// global-memory streams, two visits in flight when the policy allows it and
+// the CTA has at most 512 threads (kGlobalPairVariant), one otherwise
+// (NPMAX = 0).
 template <class M>
 int pick_npmax(const mcgb_batch_window &w)
 {
@@ -213,6 +215,8 @@ int pick_npmax(const mcgb_batch_window &w)
     }
     if (npl <= 2LL * w.threads && w.threads <= window_max_threads<M, 2>()) return 2;
     if (npl <= w.threads && w.threads <= window_max_threads<M, 1>()) return 1;
+    if (M::kGlobalInFlight == 2 && w.threads <= window_max_threads<M, kGlobalPairVariant>())
+        return kGlobalPairVariant;
     return 0;
 }
 
@@ -223,6 +227,9 @@ int launch_any(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s, c
     switch (pick_npmax<M>(w)) {
     case 1: return launch_window<M, 1>(a, w, s, name);
     case 2: return launch_window<M, 2>(a, w, s, name);
+    case kGlobalPairVariant:
+        if constexpr (M::kGlobalInFlight == 2) return launch_window<M, kGlobalPairVariant>(a, w, s, name);
+        return launch_window<M, 0>(a, w, s, name);
     default: return launch_window<M, 0>(a, w, s, name);
     }
 }
@@ -268,6 +275,12 @@ int max_clusters_any(int C, int threads, size_t smem, int *out)
     if (threads <= window_max_threads<M, 2>()) {
         if (int st = max_clusters_for<M, 2>(C, threads, smem, &n)) return st;
         if (n < best) best = n;
+    }
+    if constexpr (M::kGlobalInFlight == 2) {
+        if (threads <= window_max_threads<M, kGlobalPairVariant>()) {
+            if (int st = max_clusters_for<M, kGlobalPairVariant>(C, threads, smem, &n)) return st;
+            if (n < best) best = n;
+        }
     }
     *out = best;
     return MCGB_OK;

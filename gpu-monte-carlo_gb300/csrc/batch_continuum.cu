@@ -52,6 +52,8 @@ struct KawamuraPolicy {
     static constexpr int kPairThreads = 256;  // two plaquettes a thread spill at 128 registers
     static constexpr bool kSplitMiddle = false;
     static constexpr bool kPipeline = true;
+    // Global-stream variant: sites whose visits one thread carries at once.
+    static constexpr int kGlobalInFlight = 1;  // as for kPairThreads
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 
@@ -432,6 +434,8 @@ struct He3Policy {
     static constexpr int kPairThreads = 256;
     static constexpr bool kSplitMiddle = true;
     static constexpr bool kPipeline = false;  // update<c>: one out-of-line visit
+    // Global-stream variant: sites whose visits one thread carries at once.
+    static constexpr int kGlobalInFlight = 1;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 

@@ -33,6 +33,8 @@ struct IsingPolicy {
     static constexpr int kPairThreads = 512;
     static constexpr bool kSplitMiddle = false;
     static constexpr bool kPipeline = true;
+    // Global-stream variant: sites whose visits one thread carries at once.
+    static constexpr int kGlobalInFlight = 2;
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
 
@@ -124,6 +126,8 @@ struct XYPolicy {
     static constexpr int kPairThreads = 512;
     static constexpr bool kSplitMiddle = false;
     static constexpr bool kPipeline = true;
+    // Global-stream variant: sites whose visits one thread carries at once.
+    static constexpr int kGlobalInFlight = 2;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 

@@ -251,7 +251,7 @@ __device__ __forceinline__ void decide_pass(const typename M::Ctx &ctx, typename
 // than the register path holds).  Each thread walks its plaquettes with the
 // streams of the next two already requested, so the loads overlap with the
 // updates instead of each visit waiting on its own.
-template <class M, int C_>
+template <class M, int C_, int IF>
 __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const typename M::Ctx &ctx,
                                                 typename M::Cell *cells, float *own, const StripCtx &g,
                                                 int64_t base, int64_t gplane, float &dacc, int &nacc)
@@ -260,6 +260,50 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
     const int T = blockDim.x;
     const ulonglong2 zero = make_ulonglong2(0, 0);
     int p = threadIdx.x;
+    if constexpr (IF == 2) {
+        // Two visits at a time (sites p and p + T; sites of a colour never
+        // interact and each keeps its own stream, so the order is free):
+        // two independent dependency chains, the next pair's streams in
+        // flight meanwhile.  Site p + T is touched only when it exists.
+        ulonglong2 c0 = p < g.NPL ? rng_g[p] : zero;
+        ulonglong2 c1 = p + T < g.NPL ? rng_g[p + T] : zero;
+#pragma unroll 1
+        for (; p < g.NPL; p += 2 * T) {
+            const int q = p + T;
+            const bool has1 = q < g.NPL;
+            const ulonglong2 n0 = p + 2 * T < g.NPL ? rng_g[p + 2 * T] : zero;
+            const ulonglong2 n1 = p + 3 * T < g.NPL ? rng_g[p + 3 * T] : zero;
+            const Site s0 = make_site(p, g.LP);
+            const Site s1 = make_site(has1 ? q : p, g.LP);
+            float *o0 = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
+            float *o1 = own + (size_t)(C_ * g.NPL + (has1 ? q : p)) * M::kOwnFloats;
+            typename M::Cell &me0 = cells[C_ * g.PS + s0.o + s0.pc];
+            typename M::Cell &me1 = cells[C_ * g.PS + s1.o + s1.pc];
+            const typename M::Prop pr0 = M::template propose<C_>(ctx, me0, o0, c0);
+            typename M::Prop pr1;
+            if (has1) pr1 = M::template propose<C_>(ctx, me1, o1, c1);
+            rng_g[p] = c0;
+            if (has1) rng_g[q] = c1;
+            float dE0, dE1;
+            const Nbrs<typename M::Cell> nb0{cells, g.PS, s0};
+            if (M::template decide<C_>(ctx, nb0, me0, o0, pr0, dE0)) {
+                dacc += dE0;
+                ++nacc;
+                push_halo<C_>(cells, g, s0, me0);
+            }
+            if (has1) {
+                const Nbrs<typename M::Cell> nb1{cells, g.PS, s1};
+                if (M::template decide<C_>(ctx, nb1, me1, o1, pr1, dE1)) {
+                    dacc += dE1;
+                    ++nacc;
+                    push_halo<C_>(cells, g, s1, me1);
+                }
+            }
+            c0 = n0;
+            c1 = n1;
+        }
+        return;
+    }
     ulonglong2 cur = p < g.NPL ? rng_g[p] : zero;
     ulonglong2 nx1 = p + T < g.NPL ? rng_g[p + T] : zero;
 #pragma unroll 1
@@ -664,15 +708,23 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
         out[(size_t)lane * x.n_temps_total + t1] = __ldcg(x.staging + (size_t)lane * n + start + w1);
 }
 
+// The global-stream variant with two visits in flight (policies with
+// kGlobalInFlight = 2): compiled for at most 512 threads, so 128 registers
+// hold both chains.
+constexpr int kGlobalPairVariant = -2;
+
 // Threads per block the NPMAX variant is compiled for: NPMAX streams of four
 // colours live in registers (16 registers per plaquette).  kMaxThreads caps
 // every variant, kPairThreads the two-plaquette one (its launch bound sets
-// the register budget: 256 threads leave 255 registers a thread).
+// the register budget: 256 threads leave 255 registers a thread).  NPMAX = 0 is the
+// global-stream variant for up to 1024 threads (64 registers), one visit at
+// a time.
 template <class M, int NPMAX>
 constexpr int window_max_threads()
 {
-    return NPMAX <= 1 ? (1024 < M::kMaxThreads ? 1024 : M::kMaxThreads)
-                      : (M::kPairThreads < M::kMaxThreads ? M::kPairThreads : M::kMaxThreads);
+    return NPMAX == kGlobalPairVariant ? (512 < M::kMaxThreads ? 512 : M::kMaxThreads)
+           : NPMAX <= 1            ? (1024 < M::kMaxThreads ? 1024 : M::kMaxThreads)
+                                   : (M::kPairThreads < M::kMaxThreads ? M::kPairThreads : M::kMaxThreads);
 }
 
 template <class M, int NPMAX>
@@ -682,6 +734,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     constexpr int NS = M::kSums;  // reduced sums (>= the kChannels output channels)
     static_assert(NS + 3 <= kRedDoubles && NS <= 32, "too many reduced sums");
     constexpr int NK = NPMAX > 0 ? NPMAX : 1;
+    constexpr int GIF = NPMAX == kGlobalPairVariant ? 2 : 1;  // global variant: visits in flight
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
@@ -831,18 +884,18 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 (void)sites;
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
-                global_rng_pass<M, 0>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
+                global_rng_pass<M, 0, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 cluster_arrive();
                 cluster_wait();
-                global_rng_pass<M, 1>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
+                global_rng_pass<M, 1, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 if (M::kSplitMiddle) {
                     cluster_arrive();
                     cluster_wait();
                 }
-                global_rng_pass<M, 2>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
+                global_rng_pass<M, 2, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 cluster_arrive();
                 cluster_wait();
-                global_rng_pass<M, 3>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
+                global_rng_pass<M, 3, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
             }
 
             comp_add(dsum, dcomp, dacc);

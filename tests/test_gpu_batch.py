@@ -115,16 +115,20 @@ def test_graph_replay_equals_direct_launches(resident, split):
     assert a.swap_counts.copy_to_host()[0].sum() == 6 * 3 + 6 * 2 + 12 + 12
 
 
-@pytest.mark.parametrize("proposal", ["uniform", "gaussian"])
-def test_xy_batch_window_matches_oracle(proposal):
+@pytest.mark.parametrize("proposal,L,cluster_size,threads",
+                         [("uniform", 32, 4, 128), ("gaussian", 32, 4, 128), ("gaussian", 64, 1, 96),
+                          ("gaussian", 128, 1, 1024)])
+def test_xy_batch_window_matches_oracle(proposal, L, cluster_size, threads):
     """One 1-sweep window per colour order against the oracle: RNG bit-exact,
-    angles within float32 rounding except rare acceptance flips."""
+    angles within float32 rounding except rare acceptance flips; streams in
+    registers (L=32), in global memory two visits at a time (L=64) and one
+    at a time (L=128)."""
     from mcgb.batch import LadderBatch
     from mcgb.models.xy.model import XYModel
-    L, temps = 32, np.array([0.7, 0.9, 1.1, 1.2])
+    temps = np.array([0.7, 0.9, 1.1, 1.2])
     init = np.random.default_rng(6).uniform(-np.pi, np.pi, (4, L, L)).astype(np.float32)
     b = LadderBatch(XYModel(), [(L, temps)], seeds=[5], exchange_interval=None, proposal=proposal,
-                    sigma0=1.1, cluster_size=4, threads=128, initial_states=[init])
+                    sigma0=1.1, cluster_size=cluster_size, threads=threads, initial_states=[init])
     b.run(1)
     ref, rr = init.copy(), oracle.rng_states(4 * L * L, 5)
     betas = (1 / temps).astype(np.float32)
@@ -359,15 +363,17 @@ def test_he3_ragged_batch_samples_match_numpy():
             np.testing.assert_allclose(last[name], want, rtol=2e-5, atol=1e-3 * Lk, err_msg=name)
 
 
-def test_streams_in_global_memory_path_is_bit_exact():
+@pytest.mark.parametrize("L,threads", [(64, 128), (64, 96), (128, 1024)])
+def test_streams_in_global_memory_path_is_bit_exact(L, threads):
     """Strips with more plaquettes than two per thread keep the RNG streams in
-    global memory (the large-L path); Ising stays bit-identical."""
+    global memory (the large-L path): two visits in flight at <= 512 threads
+    (an odd count per thread at 96), one at 1024; Ising stays bit-identical."""
     from mcgb.batch import LadderBatch
     from mcgb.models.ising.model import IsingModel
-    L, temps = 64, [2.0, 2.4]
+    temps = [2.0, 2.4]
     init = seeded_spins(np.random.default_rng(3), 2, L)
     b = LadderBatch(IsingModel(), [(L, temps)], seeds=[99], exchange_interval=None, cluster_size=1,
-                    threads=128, initial_states=[init])
+                    threads=threads, initial_states=[init])
     b.run(12)
     rt = dropin_ising(L, temps, 99, init)
     for _ in range(12):
