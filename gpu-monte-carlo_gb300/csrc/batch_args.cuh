@@ -202,8 +202,8 @@ int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s
 // preferring the two-plaquette variant (compiled for fewer threads, so with
 // the larger register budget) whenever the thread count allows it; else the
 // global-memory streams, two visits in flight when the policy allows it and
-// the CTA has at most 512 threads (kGlobalPairVariant), one otherwise
-// (NPMAX = 0).
+// the CTA has at most kPairThreads threads (kGlobalPairVariant), one
+// otherwise (NPMAX = 0).
 template <class M>
 int pick_npmax(const mcgb_batch_window &w)
 {

@@ -53,7 +53,7 @@ struct KawamuraPolicy {
     static constexpr bool kSplitMiddle = false;
     static constexpr bool kPipeline = true;
     // Global-stream variant: sites whose visits one thread carries at once.
-    static constexpr int kGlobalInFlight = 1;  // as for kPairThreads
+    static constexpr int kGlobalInFlight = 2;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 

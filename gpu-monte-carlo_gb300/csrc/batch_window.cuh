@@ -709,8 +709,9 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
 }
 
 // The global-stream variant with two visits in flight (policies with
-// kGlobalInFlight = 2): compiled for at most 512 threads, so 128 registers
-// hold both chains.
+// kGlobalInFlight = 2): like the two-plaquette variant it carries two visits
+// per thread, so it shares that variant's thread cap (kPairThreads) and
+// register budget.
 constexpr int kGlobalPairVariant = -2;
 
 // Threads per block the NPMAX variant is compiled for: NPMAX streams of four
@@ -722,9 +723,8 @@ constexpr int kGlobalPairVariant = -2;
 template <class M, int NPMAX>
 constexpr int window_max_threads()
 {
-    return NPMAX == kGlobalPairVariant ? (512 < M::kMaxThreads ? 512 : M::kMaxThreads)
-           : NPMAX <= 1            ? (1024 < M::kMaxThreads ? 1024 : M::kMaxThreads)
-                                   : (M::kPairThreads < M::kMaxThreads ? M::kPairThreads : M::kMaxThreads);
+    return NPMAX <= 1 && NPMAX != kGlobalPairVariant ? (1024 < M::kMaxThreads ? 1024 : M::kMaxThreads)
+                                                    : (M::kPairThreads < M::kMaxThreads ? M::kPairThreads : M::kMaxThreads);
 }
 
 template <class M, int NPMAX>

@@ -266,16 +266,19 @@ def test_kawamura_batch_sweep_matches_oracle_and_tracks_energy():
     assert set(np.unique(st[..., 1])) <= {-1.0, 1.0}
 
 
-def test_kawamura_gaussian_batch_sweep_matches_oracle():
+@pytest.mark.parametrize("L,cluster_size,threads", [(32, 2, 256), (32, 1, 64), (96, 2, 512)])
+def test_kawamura_gaussian_batch_sweep_matches_oracle(L, cluster_size, threads):
     """Gaussian proposals (theta and d) against the oracle's restatement:
-    streams bit-exact (five draws per visit), sites within float32 rounding."""
+    streams bit-exact (five draws per visit), sites within float32 rounding;
+    streams in registers, in global memory two visits at a time (64
+    threads) and one at a time (512)."""
     from mcgb.batch import LadderBatch
     from mcgb.models.kawamura.model import KawamuraModel
-    L, temps = 32, np.linspace(0.65, 0.8, 4)
+    temps = np.linspace(0.65, 0.8, 4)
     init = npref.random_kawamura(np.random.default_rng(19), 4, L)
     sig = np.array([0.5, 0.6, 0.7, 0.8], np.float32)
     b = LadderBatch(KawamuraModel(), [(L, temps)], seeds=[18], exchange_interval=None, proposal="gaussian",
-                    cluster_size=2, threads=256, initial_states=[init])
+                    cluster_size=cluster_size, threads=threads, initial_states=[init])
     b.sigma_t.copy_to_device(sig)
     e0 = b.energies.copy_to_host()
     b.run(2)
