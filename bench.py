@@ -259,7 +259,10 @@ def run_mcgb(args, rank, world):
     batch = LadderBatch(XYModel(J=1.0), [(L, temps)], seeds=[seed], exchange_interval=EXCHANGE_INTERVAL,
                         proposal="gaussian", sigma0=1.0, initial_states=[initial_angles(seed)],
                         resident=not args.no_resident)
-    batch.autotune()
+    if args.shape:
+        batch.configure(*(int(x) for x in args.shape.split(",")))
+    else:
+        batch.autotune()
     # Warm-up: thermalise and tune the proposal widths (adaptation stops here).
     batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=True)
     sigma = batch.sigma_t.copy_to_host()
@@ -717,6 +720,9 @@ def main():
     ap.add_argument("--profile-shape", default="4,1024", help="cluster_size,threads for --profile")
     ap.add_argument("--no-resident", action="store_true",
                     help="one launch per window instead of resident multi-window launches (for profiling)")
+    ap.add_argument("--shape", default=None,
+                    help="cluster_size,threads instead of autotuning (a profiler's per-launch overhead "
+                         "would mislead the autotuner's timings)")
     ap.add_argument("--workload", default="xy-pt-l128",
                     choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "kawamura-l96x64-reference-proposals",
                              "he3-ragged", "fss-ising", "fss-xy"],
