@@ -394,7 +394,11 @@ class LadderBatch:
             npl_max = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in Ls)
             t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512,
                      MODEL_KAWAMURA_GAUSS: 512}.get(self.model_id, 1024)
-            for T in (128, 256, 512, 1024):
+            # Powers of two, and multiples of 96 for sizes whose plaquette
+            # counts carry a factor of 3 (L = 48, 96, ...): a thread count
+            # that divides a colour's plaquettes keeps every thread's share
+            # equal, so no warp idles at the colour barriers.
+            for T in (96, 128, 192, 256, 288, 384, 512, 576, 768, 1024):
                 if T > t_max or (T > 32 * ((npl_max + 31) // 32) and T > 128):
                     continue
                 out.append((C, T))

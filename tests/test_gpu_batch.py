@@ -23,7 +23,7 @@ def seeded_spins(rng, R, L):
     return rng.choice(np.array([-1, 1], dtype=np.int8), (R, L, L))
 
 
-@pytest.mark.parametrize("cluster_size,threads", [(1, 256), (2, 512), (4, 1024), (8, 128)])
+@pytest.mark.parametrize("cluster_size,threads", [(1, 256), (2, 512), (4, 1024), (8, 128), (2, 96), (1, 288)])
 def test_ising_batch_bit_exact_with_dropin_runtime(cluster_size, threads):
     from mcgb.batch import LadderBatch
     from mcgb.models.ising.model import IsingModel
