@@ -60,7 +60,31 @@ SIGNATURES = {
     "mcgb_batch_clock_tick": [_P, _I, _I, _P],
     "mcgb_batch_tune_sigma": [_P, _P, _P, _P, _P, _I, _I, _F, _F, _F, _F, _P],
     "mcgb_batch_window_exchange_noalloc": [_I, _P, _P, _P],
+    # handle API
+    "mc_create": [_I, _P, _P, _I, _P, _U64, _P, _P],
+    "mc_sweep": [_P, _I],
+    "mc_update_color": [_P, _I],
+    "mc_energy": [_P, _P],
+    "mc_measure": [_P, _P, _P, _P],
+    "mc_exchange": [_P, _I, _I64],
+    "mc_rng_init": [_P, _U64, _U64],
+    "mc_get_error": [_P],
+    "mc_copy_in": [_P, _I, _P, _I64],
+    "mc_copy_out": [_P, _I, _P, _I64],
+    "mc_destroy": [_P],
 }
+
+
+class MCParams(ctypes.Structure):
+    """ctypes mirror of ``mc_params`` (include/mcgb.h)."""
+
+    _fields_ = [("J", ctypes.c_float), ("delta", ctypes.c_float), ("sigmas", ctypes.c_void_p),
+                ("coefficients", ctypes.c_float * 5), ("K", ctypes.c_float), ("g_d", ctypes.c_float),
+                ("rho", ctypes.c_float), ("mass", ctypes.c_float)]
+
+
+# Buffers of mc_copy_in / mc_copy_out.
+MC_STATE, MC_RNG, MC_BETAS, MC_ENERGIES, MC_W2T, MC_T2W, MC_SWAP_COUNTS, MC_TRIPS, MC_EXCHANGE_RNG = range(9)
 
 # Entry points whose return value is not an int status.
 RESTYPES = {

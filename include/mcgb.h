@@ -166,6 +166,76 @@ int mcgb_pt_exchange(const double *energies, float *betas, int32_t *walker_to_te
 int mcgb_pt_record_walkers(const int32_t *walker_to_temperature, const int32_t *walker_ids,
                            int32_t *history_row, int n, void *stream);
 
+/* ------------------------------------------------------------ Handle API
+ * One reference Runtime (core/runtime.py:8-135) with its ParallelTempering
+ * state (core/parallel_tempering.py:94-317) behind an opaque handle that
+ * owns its device buffers, for C callers that want the reference's object
+ * model instead of raw kernels.  Replicas may differ in L (runs of equal L
+ * in table order).  Every call is asynchronous on the handle's stream (but
+ * mc_create, mc_copy_in/out and mc_destroy, which synchronise it) and
+ * returns MCGB_OK or a negative status; mc_get_error repeats the handle's
+ * last status, mcgb_last_error() the message.  Models: MCGB_MODEL_ISING,
+ * _XY (uniform, or Gaussian with params->sigmas), _KAWAMURA, _HE3 and
+ * _HE3_GAUSS. */
+typedef struct mc_handle mc_handle;
+
+typedef struct mc_params {
+    float J;                  /* coupling (Ising, XY, Kawamura) */
+    float delta;              /* uniform proposal width (XY, Kawamura) / He3 Cartesian step */
+    const float *sigmas;      /* XY: host (R,) Gaussian widths per replica, NULL = uniform delta */
+    float coefficients[5];    /* He3: GL betas */
+    float K, g_d;             /* He3: gradient coupling, dipole */
+    float rho, mass;          /* He3 conditional Gaussian sampler */
+} mc_params;
+
+enum {
+    MC_STATE = 0,         /* reference layout, runs concatenated: int8 / float / 5 floats / 6 floats a site */
+    MC_RNG = 1,           /* 16-byte streams, stream index = global site index */
+    MC_BETAS = 2,         /* float (R,), walker order */
+    MC_ENERGIES = 3,      /* double (R,), walker order, as of the last mc_energy / mc_exchange */
+    MC_W2T = 4,           /* int32 (R,) walker_to_temperature */
+    MC_T2W = 5,           /* int32 (R,) temperature_to_walker */
+    MC_SWAP_COUNTS = 6,   /* int64 (3, R-1) attempts, accepted, nonfinite */
+    MC_TRIPS = 7,         /* int64 (5, R) round-trip bookkeeping */
+    MC_EXCHANGE_RNG = 8,  /* 16-byte streams (R-1,), one per neighbouring pair */
+};
+
+/* Runtime(model, L, temperatures, seed) + ParallelTempering(seed + 1):
+ * site streams seeded with `seed` (stream = global site index), exchange
+ * streams with seed + 1, betas 1/T, identity maps, the ordered state (Ising
+ * +1, XY 0, Kawamura theta 0, tau +1, d = z; He3 zero) until mc_copy_in.
+ * stream NULL: the legacy default stream. */
+int mc_create(int model_id, const mc_params *params, const int32_t *L_table, int R,
+              const double *temperatures, uint64_t seed, void *stream, mc_handle **out);
+/* n_sweeps sweeps, colours 0, 1, 2, 3 each (core/runtime.py:87-99). */
+int mc_sweep(mc_handle *h, int n_sweeps);
+/* One colour of every replica (Model.update_color, core/model.py:16-23). */
+int mc_update_color(mc_handle *h, int color);
+/* Energies (R,) float64 in walker order into device `out`, or into the
+ * handle's MC_ENERGIES buffer when out is NULL (Model.measure_energy). */
+int mc_energy(mc_handle *h, double *out);
+/* Model.measure: out device (channels, R) float64; temperature_index
+ * (device, int32 (R,), nullable) puts walker w's values in column
+ * temperature_index[w]; cached_energy (device, float64 (R,) walker order,
+ * nullable) replaces the energy channel (core/model.py:25-48).  Channels:
+ * Ising 2, XY 5, Kawamura 7, He3 10 (mcgb_batch_channels). */
+int mc_measure(mc_handle *h, const int32_t *temperature_index, const double *cached_energy,
+               double *out);
+/* One exchange round at `parity` after sweep `sweep`: the energies, then
+ * core/parallel_tempering.py:35-91 on the handle's maps and counters. */
+int mc_exchange(mc_handle *h, int parity, int64_t sweep);
+/* Reseed the site streams: create_xoroshiro128p_states(sites, seed,
+ * subsequence) (core/runtime.py:51-53). */
+int mc_rng_init(mc_handle *h, uint64_t seed, uint64_t subsequence);
+/* The handle's last status (MCGB_EINVAL for a NULL handle). */
+int mc_get_error(const mc_handle *h);
+/* Synchronous host copies of a buffer (MC_STATE ... MC_EXCHANGE_RNG); n_bytes
+ * must equal its size. */
+int mc_copy_in(mc_handle *h, int buffer, const void *host, int64_t n_bytes);
+int mc_copy_out(mc_handle *h, int buffer, void *host, int64_t n_bytes);
+/* Frees the handle and its buffers (after its stream's work). */
+int mc_destroy(mc_handle *h);
+
 /* ------------------------------------------------------------ Batched engine
  * No single reference counterpart: these run what the reference does with
  * one Runtime per (L, ladder) and four launches per sweep

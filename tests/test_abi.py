@@ -15,7 +15,7 @@ HEADER = ROOT / "include" / "mcgb.h"
 def declared_functions():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mcgb_[a-z0-9_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b((?:mcgb|mc)_[a-z0-9_]+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")
@@ -33,7 +33,7 @@ def test_header_declares_the_entry_points():
 def test_library_exports_every_declared_symbol(lib):
     from mcgb import _lib
     out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.lib_path())], capture_output=True, text=True)
-    exported = set(re.findall(r"\bT (mcgb_[a-z0-9_]+)$", out.stdout, flags=re.M))
+    exported = set(re.findall(r"\bT ((?:mcgb|mc)_[a-z0-9_]+)$", out.stdout, flags=re.M))
     missing = [n for n in declared_functions() if n not in exported]
     assert not missing, f"declared but not exported: {missing}"
 
@@ -56,3 +56,13 @@ def test_argument_validation_without_a_gpu(lib):
     assert lib.mcgb_batch_channels(1) == 5 and lib.mcgb_batch_channels(4) == 10
     assert lib.mcgb_batch_channels(9) == _lib.EINVAL
     assert lib.mcgb_version().decode().startswith("mcgb")
+    # handle API: rejected before any allocation
+    h = ctypes.c_void_p()
+    params = _lib.MCParams(J=1.0, delta=1.5)
+    Ls = (ctypes.c_int32 * 2)(16, 16)
+    temps = (ctypes.c_double * 2)(1.0, 2.0)
+    assert lib.mc_create(9, ctypes.byref(params), Ls, 2, temps, 1, None, ctypes.byref(h)) == _lib.EINVAL
+    assert "per-colour form" in _lib.last_error() and not h.value
+    assert lib.mc_create(0, ctypes.byref(params), Ls, 0, temps, 1, None, ctypes.byref(h)) == _lib.EINVAL
+    assert lib.mc_get_error(None) == _lib.EINVAL and lib.mc_destroy(None) == 0
+    assert lib.mc_sweep(None, 1) == _lib.EINVAL
