@@ -72,6 +72,26 @@ def ising_observables(samples, L, temperatures, block_size=100):
     return dict(zip(("energy", "magnetization", "heat_capacity", "susceptibility", "binder"), zip(value, error)))
 
 
+def kawamura_observables(samples, L, temperatures, J=1.0, block_size=100):
+    """Energy per site, the chirality, phase and spin order parameters and
+    the helicity modulus (models/kawamura/analysis.py:33-78 estimators, from
+    per-sample squared order parameters over N^2 = L^4)."""
+    T = np.asarray(temperatures, dtype=np.float64)
+    s = {k: np.asarray(v, dtype=np.float64) for k, v in samples.items()}
+    tau2 = s["chirality"] ** 2 / L ** 4
+    phase2 = (s["px"] ** 2 + s["py"] ** 2) / L ** 4
+    spin2 = s["spin2"] / L ** 4
+    moments = {"e": s["energy"] / L ** 2, "tau2": tau2, "phase2": phase2, "spin2": spin2,
+               "cx": s["twist_cos_x"], "qx": s["twist_sin_x"], "qx2": s["twist_sin_x"] ** 2}
+
+    def est(m):
+        helicity = (J * m["cx"] - J ** 2 / T * (m["qx2"] - m["qx"] ** 2)) / L ** 2
+        return np.stack((m["e"], np.sqrt(m["tau2"]), np.sqrt(m["phase2"]), np.sqrt(m["spin2"]), helicity))
+
+    value, error = jackknife(moments, est, block_size)
+    return dict(zip(("energy", "chiral_order", "phase_order", "spin_order", "helicity"), zip(value, error)))
+
+
 def he3_observables(samples, L, temperatures, block_size=100):
     """Energy and density per site, |chirality / density|, phase order, the
     chirality Binder ratio, the mean helicity modulus and Qzz alignment."""
