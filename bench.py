@@ -383,6 +383,7 @@ def run_mcgb(args, rank, world):
     e2e_total = max_over_ranks(np.sum(e2e_ms), dist, "cuda")
     e2e_value = aggregate_rate(world, updates_per_step, args.steps, e2e_total)
 
+    drift = energy_drift(batch)
     # Plain FP64 form on the same ladder (one lattice per launch), bounded.
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
     # A resident launch runs a whole step (10 windows with their exchanges);
@@ -420,6 +421,7 @@ def run_mcgb(args, rank, world):
                          "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind},
             "clocks": clk,
             "gpu_launches": launches,
+            "energy_drift": drift,
             "tuned_sigma_range": [float(sigma.min()), float(sigma.max())],
         }
         if plain is not None:
@@ -635,6 +637,7 @@ def run_workload(args, rank, world):
     e2e_value = aggregate_rate(world, updates_per_step, n_e2e, max_over_ranks(np.sum(e2e_ms), dist, "cuda"))
     h2d = sum(t.numel() for t in host.values())
     d2h = sum(t.numel() for t in out.values()) + out_samples.numel()
+    drift = energy_drift(batch)
     if rank != 0:
         return None
     windows_per_step = SWEEPS_PER_STEP // win
@@ -657,6 +660,7 @@ def run_workload(args, rank, world):
                      "bytes_per_update": BYTES[kind], "peak_source": peak_kind},
         "clocks": clk,
         "gpu_launches": args.steps * batch.launches_per_step(windows_per_step),
+        "energy_drift": drift,
     }
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
@@ -668,6 +672,19 @@ def run_workload(args, rank, world):
                                 "sample": f"{sweeps} sweeps of the first ladder (L={L0}, {len(T0)} replicas), "
                                           f"reference proposals, no exchange, {dt:.1f} s"}
     return line
+
+
+def energy_drift(batch):
+    """The running energies (compensated float32 sums of accepted changes)
+    against an FP64 recompute of the same state, after the timed steps:
+    largest |drift| per site and relative to |E| over the replicas (the
+    recompute also resets the running energies)."""
+    drift = batch.recompute_energy().copy_to_host()
+    exact = batch.energies.copy_to_host()
+    sites = batch.table_host["L"].astype(np.float64) ** 2
+    return {"max_abs_per_site": float(np.max(np.abs(drift) / sites)),
+            "max_rel": float(np.max(np.abs(drift) / np.maximum(np.abs(exact), 1e-300))),
+            "note": "running compensated-float32 energy minus an FP64 recompute of the same state"}
 
 
 def profile_windows(cluster_size=4, threads=1024, workload="xy-pt-l128"):

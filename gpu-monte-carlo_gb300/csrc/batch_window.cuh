@@ -758,6 +758,10 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     for (int w = cm.work_ptr[cid]; w < cm.work_ptr[cid + 1]; ++w) {
         const int r = cm.work_idx[w];
         const mcgb_replica rep = cm.table[r];
+        // The next replica of this cluster's work list has another size: its
+        // strip layout differs, so the halo rows its strip load pushes into
+        // the neighbouring CTAs may land on cells they still write back.
+        const bool relayout = w + 1 < cm.work_ptr[cid + 1] && cm.table[cm.work_idx[w + 1]].L != rep.L;
         const int Ce = effective_cluster(rep.L, C);
         StripCtx g;
         g.LP = rep.L >> 1;
@@ -961,8 +965,10 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         }
         }
         // The epilogue's pushes land before rank 0 merges them: published by
-        // this barrier, or already by the barrier ending the last sweep.
-        if (!epilogue_pushed) cluster.sync();
+        // this barrier, or already by the barrier ending the last sweep.  The
+        // barrier also holds a replica of another size back until every CTA
+        // has written this one back.
+        if (!epilogue_pushed || (relayout && win + 1 == n_windows)) cluster.sync();
         if (rank == 0 && tid == 0) {
             FSum de, na, ex;
             for (int k = 0; k < C; ++k) {
@@ -1005,7 +1011,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         // temperature.  After the last window nothing waits: no replica runs
         // twice in a launch, so the next replica of the work list reads
         // nothing the exchange writes, and its strip load (cells and halo
-        // rows; the exchange reads neither) overlaps warp 0's exchange.
+        // rows; the exchange reads neither) overlaps warp 0's exchange.  A
+        // replica of the same size pushes only into halo rows, which the
+        // write-back does not read; one of another size waited above.
         if (win + 1 < n_windows) cluster.sync();
         }  // windows
     }

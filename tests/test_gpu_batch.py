@@ -1,6 +1,7 @@
 """Batched ladder engine against the per-colour drop-in path and the oracle."""
 
-from unittest.mock import patch  # noqa: F401
+import contextlib
+from unittest.mock import patch
 
 import numpy as np
 import pytest
@@ -182,6 +183,60 @@ def test_xy_batch_samples_match_exact_observables():
         got = np.empty(4)
         got[order] = ref[name]
         np.testing.assert_allclose(last[name], got, rtol=1e-5, atol=2e-3 * L, err_msg=name)
+
+
+def _mixed_size_batch(model, ladders, seeds, inits, clusters, shape, **kw):
+    """One group whose clusters each run a work list of several lattice
+    sizes (at most `clusters` clusters), a sample on every window's last
+    sweep."""
+    from mcgb.batch import LadderBatch
+    cap = patch.object(LadderBatch, "max_clusters", lambda self, C, T, idx=None: clusters)
+    with cap if clusters else contextlib.nullcontext():
+        b = LadderBatch(model, ladders, seeds=seeds, exchange_interval=5, initial_states=inits, **kw)
+        b.split_by_size(False)
+        b.configure(*shape)
+    b.allocate_samples(5, 5, 16)
+    return b
+
+
+def test_mixed_size_work_lists_with_window_end_samples_are_exact():
+    """A cluster whose work list holds several sizes, with the window-end
+    sample carrying the epilogue: bit-identical to one replica per cluster."""
+    from mcgb.models.ising.model import IsingModel
+    rng = np.random.default_rng(8)
+    ladders = [(L, list(np.geomspace(2.0, 2.6, 8))) for L in (16, 32, 48)]
+    seeds = [5, 6, 7]
+    inits = [seeded_spins(rng, 8, L) for L, _ in ladders]
+    mixed = _mixed_size_batch(IsingModel(), ladders, seeds, inits, 2, (2, 128))
+    assert mixed.n_clusters == 2 and not mixed.resident
+    wp, wi = mixed.work_ptr.copy_to_host(), mixed.work_idx.copy_to_host()
+    assert all(len(set(mixed.table_host["L"][wi[wp[c]:wp[c + 1]]])) > 1 for c in range(2))
+    one = _mixed_size_batch(IsingModel(), ladders, seeds, inits, None, (2, 128))
+    assert one.n_clusters == 24
+    for b in (mixed, one):
+        b.run(40)
+        b.check_errors()
+    for k in range(3):
+        np.testing.assert_array_equal(mixed.ladder_state(k), one.ladder_state(k))
+    np.testing.assert_array_equal(mixed.w2t.copy_to_host(), one.w2t.copy_to_host())
+    np.testing.assert_array_equal(mixed.samples.copy_to_host(), one.samples.copy_to_host())
+    np.testing.assert_array_equal(mixed.energies.copy_to_host(), one.energies.copy_to_host())
+    assert np.all(mixed.recompute_energy().copy_to_host() == 0.0)
+
+
+def test_he3_mixed_size_work_lists_keep_the_running_energy():
+    """He3 (float state, running float energy) on mixed-size work lists with
+    window-end samples: the running energy stays within rounding of an FP64
+    recompute of the state."""
+    from mcgb.models.he3.model import He3Model
+    T = list(np.geomspace(0.33, 0.47, 6))
+    ladders = [(L, T) for L in (32, 48, 64)]
+    b = _mixed_size_batch(He3Model(), ladders, [1, 2, 3], None, 2, (2, 256), gaussian=True)
+    b.run(60)
+    b.check_errors()
+    drift = b.recompute_energy().copy_to_host()
+    scale = np.maximum(np.abs(b.energies.copy_to_host()), b.table_host["L"].astype(np.float64) ** 2)
+    assert np.max(np.abs(drift) / scale) < 1e-5
 
 
 def test_ragged_batch_ladders_match_their_own_runtimes():
