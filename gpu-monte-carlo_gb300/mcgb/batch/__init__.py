@@ -122,6 +122,17 @@ def lpt_work_lists(costs, n_clusters):
     return ptrs, idx, loads
 
 
+def visit_costs(Ls, C, T):
+    """Relative time a cluster of C CTAs x T threads spends on each replica of
+    sizes Ls, for its work lists: the visits a thread makes per colour phase
+    (the strip's plaquettes over the threads, rounded up -- a strip smaller
+    than the block leaves threads idle, so a small lattice costs more than
+    its share of sites) plus a fixed share for the strip load, write-back
+    and exchange."""
+    npl = np.array([int(L) ** 2 // (4 * LadderBatch.effective_cluster(L, C)) for L in Ls], dtype=np.float64)
+    return np.ceil(npl / int(T)) + 0.5
+
+
 class _Group:
     """Replicas that share one cluster shape: one launch per window (or one
     resident launch of many windows) runs them.  A ladder has one lattice
@@ -409,6 +420,9 @@ class LadderBatch:
         Ls = (self.table_host["L"] if idx is None else self.table_host["L"][idx]).astype(np.int64)
         return np.array([L * L / self.effective_cluster(L, C) for L in Ls], dtype=np.float64)
 
+    def _work_costs(self, C, T, idx=None):
+        return visit_costs(self.table_host["L"] if idx is None else self.table_host["L"][idx], C, T)
+
     def max_clusters(self, C, T, idx=None):
         n = ctypes.c_int(0)
         _lib.call("mcgb_batch_max_clusters", self.model_id, C, T, self._smem(C, idx), ctypes.byref(n))
@@ -455,7 +469,7 @@ class LadderBatch:
         if m < 1:
             raise ValueError(f"cluster shape ({C}, {T}) cannot be resident")
         g.cluster_size, g.threads, g.n_clusters = C, T, min(m, len(idx))
-        wp, wi, _ = lpt_work_lists(self._costs(C, idx), g.n_clusters)
+        wp, wi, _ = lpt_work_lists(self._work_costs(C, T, idx), g.n_clusters)
         g.work_host = np.ascontiguousarray(idx[wi].astype(np.int32))
         g.work_ptr, g.work_idx = to_device(wp), to_device(g.work_host)
         # Resident launches (many windows per launch, strips kept on chip)

@@ -181,3 +181,17 @@ def test_invalid_history_is_rejected():
     run["metadata"]["parallel_tempering"]["walker_history"] = {
         "walker_ids": [0, 2], "sweeps": [10, 20], "temperature_indices": [[0, 1], [1, 2]]}
     assert pt_analysis.pt_summary({16: run})[16]["history_available"]
+
+
+def test_work_lists_cost_visits_per_thread():
+    """Work lists weigh a replica by the visits each thread makes per colour
+    phase, so a lattice smaller than the block is not taken for nearly free:
+    on 4 x 256, L=32 (64 plaquettes a CTA) costs one visit, L=128 four."""
+    from mcgb.batch import lpt_work_lists, visit_costs
+    Ls = np.repeat([32, 128], 4)
+    costs = visit_costs(Ls, 4, 256)
+    assert list(costs) == [1.5] * 4 + [4.5] * 4
+    wp, wi, loads = lpt_work_lists(costs, 4)
+    for k in range(4):
+        assert sorted(Ls[wi[wp[k]:wp[k + 1]]]) == [32, 128]
+    np.testing.assert_allclose(loads, 6.0)
