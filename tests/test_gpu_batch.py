@@ -118,12 +118,12 @@ def test_graph_replay_equals_direct_launches(resident, split):
 
 @pytest.mark.parametrize("proposal,L,cluster_size,threads",
                          [("uniform", 32, 4, 128), ("gaussian", 32, 4, 128), ("gaussian", 64, 1, 96),
-                          ("gaussian", 128, 1, 1024)])
+                          ("gaussian", 128, 1, 1024), ("gaussian", 512, 16, 1024)])
 def test_xy_batch_window_matches_oracle(proposal, L, cluster_size, threads):
     """One 1-sweep window per colour order against the oracle: RNG bit-exact,
     angles within float32 rounding except rare acceptance flips; streams in
     registers (L=32), in global memory two visits at a time (L=64) and one
-    at a time (L=128)."""
+    at a time (L=128, and L=512 on 16 CTAs: four plaquettes a thread)."""
     from mcgb.batch import LadderBatch
     from mcgb.models.xy.model import XYModel
     temps = np.array([0.7, 0.9, 1.1, 1.2])
@@ -421,16 +421,19 @@ def test_he3_ragged_batch_samples_match_numpy():
             np.testing.assert_allclose(last[name], want, rtol=2e-5, atol=1e-3 * Lk, err_msg=name)
 
 
-@pytest.mark.parametrize("L,threads", [(64, 128), (64, 96), (128, 1024)])
-def test_streams_in_global_memory_path_is_bit_exact(L, threads):
+@pytest.mark.parametrize("L,cluster_size,threads", [(64, 1, 128), (64, 1, 96), (128, 1, 1024), (512, 2, 1024),
+                                                    (512, 16, 1024)])
+def test_streams_in_global_memory_path_is_bit_exact(L, cluster_size, threads):
     """Strips with more plaquettes than two per thread keep the RNG streams in
     global memory (the large-L path): two visits in flight at <= 512 threads
-    (an odd count per thread at 96), one at 1024; Ising stays bit-identical."""
+    (an odd count per thread at 96), one at 1024; Ising stays bit-identical,
+    up to the largest lattice of the finite-size batch (L=512, 16 and 2 CTAs
+    a replica: 4 and 32 plaquettes a thread per colour)."""
     from mcgb.batch import LadderBatch
     from mcgb.models.ising.model import IsingModel
     temps = [2.0, 2.4]
     init = seeded_spins(np.random.default_rng(3), 2, L)
-    b = LadderBatch(IsingModel(), [(L, temps)], seeds=[99], exchange_interval=None, cluster_size=1,
+    b = LadderBatch(IsingModel(), [(L, temps)], seeds=[99], exchange_interval=None, cluster_size=cluster_size,
                     threads=threads, initial_states=[init])
     b.run(12)
     rt = dropin_ising(L, temps, 99, init)
