@@ -262,7 +262,7 @@ def run_mcgb(args, rank, world):
     if args.shape:
         batch.configure(*(int(x) for x in args.shape.split(",")))
     else:
-        batch.autotune()
+        batch.autotune(sample_interval=SAMPLE_INTERVAL)
     # Warm-up: thermalise and tune the proposal widths (adaptation stops here).
     batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=True)
     sigma = batch.sigma_t.copy_to_host()
@@ -562,7 +562,10 @@ def run_workload(args, rank, world):
     batch = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
                         proposal="gaussian" if gauss else "uniform", gaussian=kind == "he3",
                         sigma0=0.5 if kind == "kawamura-gauss" else 1.0, initial_states=inits)
-    batch.autotune()
+    if args.shape:
+        batch.configure(*(int(x) for x in args.shape.split(",")))
+    else:
+        batch.autotune(sample_interval=si)
     tune = gauss
     batch.run(max(args.warmup, 3) * SWEEPS_PER_STEP, tune=tune)
     batch.allocate_samples(batch.sweeps + si, si, (args.steps + 2) * SWEEPS_PER_STEP // si)

@@ -914,14 +914,18 @@ class LadderBatch:
         }
 
     # ------------------------------------------------------------ autotuning
-    def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False, split=None):
+    def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False, split=None, sample_interval=None):
         """Time each valid (cluster_size, threads) on a copy-free trial window
         and keep the fastest, per group.  For a batch of several lattice sizes
         (`split` None) it also times one group per size and keeps that when
         its summed window time beats the best single launch by 5 %; `split`
-        True/False forces either.  State and RNG are saved and restored, so
-        tuning does not change the Markov chain.  Returns the trial times
-        [(ms, cluster_size, threads)] of the kept grouping's groups."""
+        True/False forces either.  With `sample_interval` the trial windows
+        also take samples at that cadence (into a scratch ring): a sample's
+        reduction across a cluster's CTAs costs more on larger clusters, so
+        frequent sampling can favour another shape.  State and RNG are saved
+        and restored, so tuning does not change the Markov chain.  Returns
+        the trial times [(ms, cluster_size, threads)] of the kept grouping's
+        groups."""
         n = sweeps_per_trial or (self.exchange_interval or 10)
         saved_state = self.state.raw().clone()
         saved_aux = None if self.aux is None else self.aux.raw().clone()
@@ -930,6 +934,12 @@ class LadderBatch:
         saved_acc = self.accepted.raw().clone()
         saved_clock = self.clock.raw().clone()
         saved_samples, self.samples = self.samples, None
+        saved_ring = (self.n_slots, self.first_sample_sweep, self.sample_interval)
+        if sample_interval:
+            si = int(sample_interval)
+            if si < 1:
+                raise ValueError("sample_interval must be positive")
+            self.allocate_samples(self.sweeps + si, si, n // si + 1)
 
         def tune_groups():
             total, trials = 0.0, []
@@ -966,6 +976,7 @@ class LadderBatch:
         self.accepted.raw().copy_(saved_acc)
         self.clock.raw().copy_(saved_clock)
         self.samples = saved_samples
+        self.n_slots, self.first_sample_sweep, self.sample_interval = saved_ring
         self._graphs.clear()
         self._resident_checked = False
         self.recompute_energy()

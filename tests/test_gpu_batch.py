@@ -545,3 +545,31 @@ def test_resident_wait_that_runs_out_is_reported_and_the_batch_recovers():
     w2t, t2w = b.w2t.copy_to_host(), b.t2w.copy_to_host()
     np.testing.assert_array_equal(t2w[w2t], np.arange(4))
     np.testing.assert_array_equal(b.betas.copy_to_host(), b._initial_betas[w2t])
+
+
+def test_autotune_with_samples_leaves_the_chain_and_the_ring_alone():
+    """Autotuning with a sample cadence times its trials with a scratch ring,
+    then restores the caller's ring and the chain: the run afterwards equals
+    an untuned twin's on the same shape, samples included."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    init = seeded_spins(np.random.default_rng(12), 4, 32)
+    kw = dict(seeds=[21], exchange_interval=5, initial_states=[init])
+    a = LadderBatch(IsingModel(), [(32, np.geomspace(2.0, 2.6, 4))], **kw)
+    b = LadderBatch(IsingModel(), [(32, np.geomspace(2.0, 2.6, 4))], **kw)
+    for x in (a, b):
+        x.allocate_samples(5, 5, 8)
+        x.run(10)
+    before = a.samples.copy_to_host()
+    ring = (a.n_slots, a.first_sample_sweep, a.sample_interval)
+    trials = a.autotune(sample_interval=1, shapes=[(1, 128), (2, 128), (4, 64)])
+    assert len(trials) == 3 and (a.cluster_size, a.threads) in [(C, T) for _, C, T in trials]
+    assert (a.n_slots, a.first_sample_sweep, a.sample_interval) == ring
+    np.testing.assert_array_equal(a.samples.copy_to_host(), before)
+    b.configure(a.cluster_size, a.threads)
+    for x in (a, b):
+        x.run(20)
+        x.check_errors()
+    np.testing.assert_array_equal(a.ladder_state(0), b.ladder_state(0))
+    for name in ("samples", "w2t", "energies", "clock"):
+        np.testing.assert_array_equal(getattr(a, name).copy_to_host(), getattr(b, name).copy_to_host(), err_msg=name)
