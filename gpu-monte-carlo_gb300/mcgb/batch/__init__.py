@@ -780,15 +780,19 @@ class LadderBatch:
         """Asynchronous device-to-host copy of the chain state (one copy)."""
         host["chain"].copy_(self._chain_host, non_blocking=True)
 
-    def checkpoint(self):
-        """Everything needed to resume the chain bit-exactly, as host arrays."""
+    def _chain_arrays(self):
+        """Names of the device arrays that hold the chain and its bookkeeping."""
         names = ["state", "rng", "betas", "w2t", "t2w", "e_run", "energies", "accepted", "accepted_prev",
                  "clock", "sigma_t", "counters"]
         if self.aux is not None:
             names.append("aux")
         if self.pt:
             names += ["pair_rng", "swap_counts", "trips"]
-        ck = {n: getattr(self, n).copy_to_host().copy() for n in names}
+        return names
+
+    def checkpoint(self):
+        """Everything needed to resume the chain bit-exactly, as host arrays."""
+        ck = {n: getattr(self, n).copy_to_host().copy() for n in self._chain_arrays()}
         ck["sweeps"], ck["exchange_rounds"] = self.sweeps, self.exchange_rounds
         return ck
 
@@ -917,8 +921,8 @@ class LadderBatch:
     def autotune(self, sweeps_per_trial=None, shapes=None, verbose=False, split=None, sample_interval=None):
         """Time each valid (cluster_size, threads) on a copy-free trial window
         and keep the fastest, per group.  For a batch of several lattice sizes
-        (`split` None) it also times one group per size and keeps that when
-        its summed window time beats the best single launch by 5 %; `split`
+        (`split` None) it also tunes one group per size and keeps that when a
+        few real steps of it beat the single launch's by 2 %; `split`
         True/False forces either.  With `sample_interval` the trial windows
         also take samples at that cadence (into a scratch ring): a sample's
         reduction across a cluster's CTAs costs more on larger clusters, so
@@ -956,13 +960,25 @@ class LadderBatch:
             one_shape = (self.cluster_size, self.threads)
             self.split_by_size(True)
             many, many_trials = tune_groups()
+            many_shapes = [(g.cluster_size, g.threads) for g in self.groups]
+            # Trial windows launch every group once per window; a production
+            # step replays graphs of resident launches, which hide most of
+            # that cost.  So the grouping is chosen on a few real steps.
+            many_run = self._time_steps(n)
+            self.split_by_size(False)
+            self.configure(*one_shape)
+            one_run = self._time_steps(n)
             if verbose:
-                print(f"autotune: one launch {one:.3f} ms, one per size {many:.3f} ms per {n}-sweep window")
-            if many < 0.95 * one:
+                print(f"autotune: one launch {one:.3f} ms, one per size {many:.3f} ms per {n}-sweep window "
+                      f"(trials); {one_run:.3f} ms against {many_run:.3f} ms (steps)")
+            if many_run < 0.98 * one_run:
+                self.split_by_size(True)
+                for g, (C, T) in zip(self.groups, many_shapes):
+                    self._configure_group(g, C, T)
+                self._graphs.clear()
+                self._resident_checked = False
                 results = many_trials
             else:
-                self.split_by_size(False)
-                self.configure(*one_shape)
                 results = one_trials
         else:
             if split is not None and ragged and split != (len(self.groups) > 1):
@@ -981,6 +997,36 @@ class LadderBatch:
         self._resident_checked = False
         self.recompute_energy()
         return results
+
+    def _time_steps(self, n, windows=8):
+        """ms per n-sweep window of `windows` windows run as production runs
+        them (graph replay, resident launches, exchanges), after a warm-up of
+        the same plan, which captures the graphs the timed run replays.
+        Everything the run changes is put back."""
+        kept = {name: getattr(self, name).raw().clone() for name in self._chain_arrays()}
+        sweeps, rounds = self.sweeps, self.exchange_rounds
+        self._graphs.clear()
+        self._resident_checked = False
+        self.run(windows * n)
+        self.run(windows * n)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        self.run(windows * n)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / windows
+        self.check_errors()
+        for name, raw in kept.items():
+            getattr(self, name).raw().copy_(raw)
+        self.sweeps, self.exchange_rounds = sweeps, rounds
+        if self.pt:
+            # decision words of the rounds just run would match the same
+            # rounds run again
+            self.sync.copy_to_device(np.zeros(len(self.sync), np.int32))
+        self._graphs.clear()
+        self._resident_checked = False
+        return ms
 
     def _tune_group(self, g, n, shapes=None, verbose=False):
         """Time group g's window over its candidate shapes; keep the fastest."""

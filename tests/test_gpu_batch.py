@@ -573,3 +573,36 @@ def test_autotune_with_samples_leaves_the_chain_and_the_ring_alone():
     np.testing.assert_array_equal(a.ladder_state(0), b.ladder_state(0))
     for name in ("samples", "w2t", "energies", "clock"):
         np.testing.assert_array_equal(getattr(a, name).copy_to_host(), getattr(b, name).copy_to_host(), err_msg=name)
+
+
+def test_autotune_of_a_ragged_batch_times_real_steps_and_puts_everything_back():
+    """Choosing between one launch and one launch per size runs a few real
+    steps of each (exchanges, resident launches, graphs); afterwards the chain
+    continues exactly as an untuned twin's with the grouping and shapes
+    autotune chose: states, maps, counters, round trips, samples, clock."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.ising.model import IsingModel
+    rng = np.random.default_rng(31)
+    ladders = [(16, list(np.geomspace(2.0, 2.6, 6))), (32, list(np.geomspace(2.0, 2.6, 5)))]
+    inits = [seeded_spins(rng, len(T), L) for L, T in ladders]
+    kw = dict(seeds=[8, 9], exchange_interval=5, initial_states=inits)
+    a = LadderBatch(IsingModel(), ladders, **kw)
+    b = LadderBatch(IsingModel(), ladders, **kw)
+    for x in (a, b):
+        x.allocate_samples(5, 5, 16)
+        x.run(10)
+    a.autotune(sample_interval=5, shapes=[(1, 128), (2, 128)])
+    if len(a.groups) > 1:
+        b.split_by_size(True)
+    for ga, gb in zip(a.groups, b.groups):
+        b._configure_group(gb, ga.cluster_size, ga.threads)
+    b._graphs.clear()
+    assert [list(ga.idx) for ga in a.groups] == [list(gb.idx) for gb in b.groups]
+    for x in (a, b):
+        x.run(30)
+        x.check_errors()
+    for k in range(2):
+        np.testing.assert_array_equal(a.ladder_state(k), b.ladder_state(k))
+    for name in ("w2t", "t2w", "betas", "swap_counts", "trips", "energies", "clock", "samples"):
+        np.testing.assert_array_equal(getattr(a, name).copy_to_host(), getattr(b, name).copy_to_host(), err_msg=name)
+    assert a.sweeps == b.sweeps == 40 and a.exchange_rounds == b.exchange_rounds == 8
