@@ -365,13 +365,18 @@ typedef struct mcgb_batch_pt {
 int mcgb_batch_exchange(const mcgb_batch_window *w, const mcgb_batch_pt *pt, void *stream);
 /* No counterpart in the reference.  mcgb_batch_window_run then
  * mcgb_batch_exchange in one call that allocates nothing, for callers that
- * cannot allocate device memory (inside a CUDA-graph capture, or under a
- * runtime that owns every device allocation).  w->staging must be NULL: the
- * deferred-sample scratch is a fixed array in the library of 32768 doubles,
- * so channels x n_replicas must not exceed 32768 (else MCGB_EINVAL).  All
- * calls share that array: calls that overlap on the GPU race.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  The caller ticks the clock as with the two separate calls. */
+ * cannot allocate device memory: a program inside a host runtime that owns
+ * every device allocation (a pool sized to the whole GPU, or a binding whose
+ * allocator must not be bypassed), or a latency-critical loop that cannot
+ * afford cudaMalloc's implicit device synchronisation.  w->staging must be
+ * NULL: the deferred-sample scratch is a fixed array in the library of 32768
+ * doubles, so channels x n_replicas must not exceed 32768 (else MCGB_EINVAL).
+ * One launch over the whole replica table only: host_work_idx NULL, n_work 0
+ * and hold_clock 0 (size-group windows are rejected with MCGB_EINVAL).  All
+ * calls on one device share that array and must not overlap on the GPU
+ * (serialise them on one stream); each device has its own copy.  The first
+ * call in a CUDA context looks up the array's address; make it before any
+ * stream capture.  The caller ticks the clock as with the two separate calls. */
 int mcgb_batch_window_exchange_noalloc(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                        void *stream);
 /* No counterpart in the reference (it launches four colour kernels per sweep

@@ -1,9 +1,10 @@
 """The allocation-free window + exchange entry point.
 
-Callers that cannot allocate device memory (a C-ABI client inside a CUDA
-graph capture, or an embedding runtime that owns every device allocation)
-use mcgb_batch_window_exchange_noalloc, whose deferred-sample scratch is a
-fixed array inside the library.  Two identical batches advance side by side,
+Callers that cannot allocate device memory (a program inside a host runtime
+that owns every device allocation, or a latency-critical loop that cannot
+take cudaMalloc's implicit device synchronisation) use
+mcgb_batch_window_exchange_noalloc, whose deferred-sample scratch is a fixed
+array inside the library.  Two identical batches advance side by side,
 one through the existing two calls with caller-allocated scratch and one
 through the new entry point; after each of two calls in a row their states,
 samples, maps, counters and energies must agree exactly (the same kernels run
@@ -75,5 +76,25 @@ def test_noalloc_window_rejects_oversized_batches_and_caller_scratch():
     w = b._window(5, staging=False)
     w.n_replicas = 7000  # 7000 x 5 channels > 32768 (checked before any launch)
     with pytest.raises(ValueError, match="exceed the fixed scratch"):
+        _lib.call("mcgb_batch_window_exchange_noalloc", b.model_id, ctypes.byref(w), ctypes.byref(b._pt()),
+                  _lib.stream_handle())
+
+
+def test_noalloc_window_rejects_size_group_windows():
+    # A window over one size group covers part of the table; the exchange
+    # would then read scratch entries of other replicas that this call never
+    # wrote, so the entry point refuses it before any launch.
+    from mcgb import _lib
+    b = make_batch()
+    work = np.arange(6, dtype=np.int32)
+    w = b._window(5, staging=False)
+    w.host_work_idx = work.ctypes.data
+    w.n_work = len(work)
+    with pytest.raises(ValueError, match="whole replica table"):
+        _lib.call("mcgb_batch_window_exchange_noalloc", b.model_id, ctypes.byref(w), ctypes.byref(b._pt()),
+                  _lib.stream_handle())
+    w = b._window(5, staging=False)
+    w.hold_clock = 1
+    with pytest.raises(ValueError, match="hold_clock must be 0"):
         _lib.call("mcgb_batch_window_exchange_noalloc", b.model_id, ctypes.byref(w), ctypes.byref(b._pt()),
                   _lib.stream_handle())
