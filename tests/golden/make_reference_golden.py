@@ -1,6 +1,7 @@
 """Golden vectors produced by the reference's own Python code.
 
-    python tests/golden/make_reference_golden.py   (needs the reference checkout)
+    python tests/golden/make_reference_golden.py --reference <checkout>
+    (or set MCGB_REFERENCE to the checkout)
 
 The reference's run-file writer (utils/data_io.py) and temperature-ladder
 builder (utils/temperature_ladder.py) import only numpy and json, so they run
@@ -14,14 +15,15 @@ here as they are.  This script imports them from the checkout and writes
   read back exactly.
 """
 
+import argparse
 import json
+import os
 import sys
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path("/root/reference")
 
 LADDERS = [
     {"T_min": 0.70, "T_max": 1.20, "n_T": 32},
@@ -64,9 +66,15 @@ def sample_runs():
 
 
 def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--reference", default=os.environ.get("MCGB_REFERENCE"),
+                    help="path of the reference checkout (or MCGB_REFERENCE)")
+    args = ap.parse_args()
+    if not args.reference:
+        ap.error("give --reference or set MCGB_REFERENCE")
     # The checkout is read-only: import it without writing bytecode there.
     sys.dont_write_bytecode = True
-    sys.path.insert(0, str(REFERENCE))
+    sys.path.insert(0, str(Path(args.reference).resolve()))
     from utils.data_io import save_runs
     from utils.temperature_ladder import make_temperature_ladder
 
