@@ -14,7 +14,11 @@ Arms:
                     replay;
   --impl reference  the reference algorithm on the host cores: the C
                     restatement of its kernels (the reference has no CPU sweep
-                    of its own), OpenMP over replicas, a bounded sample.
+                    of its own), OpenMP over replicas, a bounded sample;
+  --api dropin      the same ladder through the reference's entry points,
+                    Simulation(ParallelTempering(Runtime(XYModel()))), with
+                    the reference's update rule (per-colour kernels, uniform
+                    proposal), its schedule replayed as CUDA graphs.
 
 `value` is the production mode (updates + exchange + sampling); `modes` adds
 the same ladder with updates only and with updates + exchange.
@@ -51,6 +55,8 @@ SWEEPS_PER_STEP = 100
 BYTES_PER_UPDATE = 40      # XY: 4+4 B angle read+write, 32 B RNG stream read+write
 METRIC = "attempted spin updates/ns"
 WORKLOAD = "XY PT ladder L=128 x 32 temperatures geometric [0.70, 1.20], Gaussian MH (sigma tuned to ~50%)"
+REFERENCE_WORKLOAD = ("XY PT ladder L=128 x 32 temperatures geometric [0.70, 1.20], the reference's uniform "
+                      "proposal theta + 1.5 (2u - 1) (models/xy/update.py:6-54)")
 
 
 def temperatures():
@@ -64,22 +70,67 @@ def initial_angles(seed):
     return np.clip(theta, np.float32(-np.pi), np.nextafter(np.float32(np.pi), np.float32(0)))
 
 
-def profiled_traffic(name="window_kernel_xy_L128x32.md"):
-    """DRAM bytes per launch from a committed ncu summary of the kernel on this
-    workload (dram__bytes_read.sum + write.sum), or None."""
-    path = ROOT / "profiles" / name
-    if not path.exists():
-        return None
-    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
-    total = 0.0
-    found = 0
+PROFILE = {"xy-pt-l128": "window_kernel_xy_L128x32.md", "he3-ragged": "window_kernel_he3_ragged.md",
+           "kawamura-l96x64": "window_kernel_kawamura_L96x3072.md", "fss-ising": "window_kernel_fss_ising.md",
+           "fss-xy": "window_kernel_fss_xy.md"}
+
+
+def profile_figures(name):
+    """Figures of a committed ncu summary under profiles/ (one capture of the
+    workload's window kernel): {metric: value} for the rows whose metric name
+    is given in backticks, in base units, or {} if there is none."""
+    path = ROOT / "profiles" / name if name else None
+    if path is None or not path.exists():
+        return {}
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "inst": 1, "us": 1e-6, "ms": 1e-3}
+    out = {}
     for line in path.read_text().splitlines():
-        for key in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
-            if f"(`{key}`)" in line:
-                fields = line.split("|")[2].split()
-                total += float(fields[0]) * scale.get(fields[1] if len(fields) > 1 else "byte", 1)
-                found += 1
-    return total if found == 2 else None
+        cells = line.split("|")
+        if len(cells) < 4 or "(`" not in cells[1]:
+            continue
+        key = cells[1].split("(`")[1].split("`)")[0]
+        fields = cells[2].split()
+        try:
+            out[key] = float(fields[0].replace(",", "")) * scale.get(fields[1] if len(fields) > 1 else "", 1)
+        except (ValueError, IndexError):
+            continue
+    return out
+
+
+def roofline_line(figs, source, updates_per_launch, launch_ms, bytes_per_update, sm_mhz, kernel):
+    """The window kernel against the bound that binds it, instruction issue.
+
+    achieved = warp instructions per launch / the launch's event-timed
+    duration, where warp instructions per attempted update come from the ncu
+    capture (smsp__inst_executed.sum over the updates of the captured
+    launch); peak = SMs x 4 schedulers x 1 warp instruction per cycle x the
+    SM clock sampled during the timed region.  The algorithmic-HBM figure
+    (bytes per update x updates / duration, against the measured copy
+    bandwidth) rides along under "hbm": the kernel keeps state and streams on
+    chip, so its DRAM traffic ("traffic", per launch, from the same capture)
+    is a small fraction of the algorithmic bytes."""
+    import torch
+    peak_hbm, peak_kind = load_peaks()
+    alg = bytes_per_update * updates_per_launch / (launch_ms * 1e-3) / 1e9
+    n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    issue_peak = n_sm * 4 * sm_mhz * 1e6 / 1e9
+    traffic = None
+    if "dram__bytes_read.sum" in figs and "dram__bytes_write.sum" in figs:
+        traffic = figs["dram__bytes_read.sum"] + figs["dram__bytes_write.sum"]
+    line = {"bound": "issue", "achieved": None, "peak": issue_peak, "unit": "G warp-instructions/s",
+            "frac": None, "traffic": traffic, "kernel": kernel, "kernel_ms": launch_ms,
+            "peak_source": f"{n_sm} SMs x 4 schedulers x {sm_mhz:.0f} MHz (sampled)",
+            "hbm": {"achieved": alg, "peak": peak_hbm, "unit": "GB/s", "frac": alg / peak_hbm,
+                    "bytes_per_update": bytes_per_update, "peak_source": peak_kind,
+                    "note": "algorithmic bytes (state r+w + 32 B of RNG stream per update) over the "
+                            "kernel time; the kernel keeps them on chip, see traffic"},
+            "source": f"profiles/{source}" if figs else None}
+    if "smsp__inst_executed.sum" in figs and figs.get("updates"):
+        per_update = figs["smsp__inst_executed.sum"] / figs["updates"]
+        achieved = per_update * updates_per_launch / (launch_ms * 1e-3) / 1e9
+        line.update({"achieved": achieved, "frac": achieved / issue_peak,
+                     "warp_instructions_per_update": per_update})
+    return line
 
 
 def load_peaks():
@@ -220,7 +271,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform angles)",
-        "config": {"workload": WORKLOAD, "sweeps_per_step": sweeps, "parallelism": "host threads",
+        "config": {"workload": REFERENCE_WORKLOAD, "sweeps_per_step": sweeps, "parallelism": "host threads",
                    "step": f"a bounded sample: {sweeps} of the workload's {SWEEPS_PER_STEP} sweeps per step"},
         "cpu_baseline": {"value": value, "unit": "updates/ns", "cores": cores, "kind": "port",
                          "sample": f"{sweeps} sweeps of the 32-replica L=128 ladder per step, exchange "
@@ -349,9 +400,14 @@ def run_mcgb(args, rank, world):
     torch.cuda.synchronize()
     launch_ms = k0.elapsed_time(k1) / reps
     window_ms = launch_ms / windows
-    alg_bytes = BYTES_PER_UPDATE * N_TEMPS * L * L * EXCHANGE_INTERVAL * windows
-    peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    sm_mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    roofline = roofline_line(profile_figures(PROFILE["xy-pt-l128"]), PROFILE["xy-pt-l128"],
+                             N_TEMPS * L * L * EXCHANGE_INTERVAL * windows, launch_ms, BYTES_PER_UPDATE, sm_mhz,
+                             "window_kernel<XYPolicy>" + (" (resident, %d windows)" % windows
+                                                          if batch.resident else ""))
+    roofline["window_ms"] = window_ms
+    roofline["traffic_note"] = ("DRAM bytes of one ncu capture of a one-window launch: the strip is loaded and "
+                                "written back once per launch, resident or not")
 
     # End to end through the public API with host buffers: every step uploads
     # the chain state (angles, RNG streams, (cos, sin) cache, running
@@ -386,6 +442,8 @@ def run_mcgb(args, rank, world):
     drift = energy_drift(batch)
     # Plain FP64 form on the same ladder (one lattice per launch), bounded.
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
+    # The reference-facing entry points on the same ladder, bounded.
+    dropin = dropin_rate(20 * SWEEPS_PER_STEP, seed)[0] if rank == 0 else None
     # A resident launch runs a whole step (10 windows with their exchanges);
     # otherwise one fused launch per window.
     launches = args.steps * batch.launches_per_step(SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
@@ -407,18 +465,7 @@ def run_mcgb(args, rank, world):
                     "d2h_bytes_per_step": int(d2h)},
             "modes": {"updates": updates_rate, "pt": pt_rate, "production": value,
                       "unit": "updates/ns", "note": "updates only / + exchange every 10 / + sample every 10"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
-                         # The strip's load and write-back happen once per launch, resident or
-                         # not: the one-window capture's DRAM bytes stand for either launch.
-                         "traffic": profiled_traffic(),
-                         "traffic_source": "profiles/window_kernel_xy_L128x32.md (one ncu capture of a "
-                                           "one-window launch; the strip is loaded and written back once per "
-                                           "launch in both forms)",
-                         "kernel": "window_kernel<XYPolicy>" + (" (resident, %d windows)" % windows
-                                                                if batch.resident else ""),
-                         "kernel_ms": launch_ms, "window_ms": window_ms,
-                         "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind},
+            "roofline": roofline,
             "clocks": clk,
             "gpu_launches": launches,
             "energy_drift": drift,
@@ -426,25 +473,101 @@ def run_mcgb(args, rank, world):
         }
         if plain is not None:
             line["plain_fp64"] = {"value": plain, "unit": "updates/ns",
-                                  "form": "one lattice per launch, float64 state and arithmetic"}
+                                  "form": "one lattice per launch, float64 state and arithmetic, each "
+                                          "exchange interval's launches replayed from a CUDA graph"}
             line["speedup_vs_plain_fp64"] = value / plain
+        if dropin is not None:
+            line["dropin"] = {"value": dropin, "unit": "updates/ns",
+                              "form": "Simulation(ParallelTempering(Runtime(XYModel()))).run(), the reference's "
+                                      "uniform proposal and per-colour kernels, schedule replayed as CUDA "
+                                      "graphs, 2000 sweeps (bench.py --api dropin times it alone)"}
     return line
+
+
+def dropin_rate(sweeps, seed, host_inputs=False):
+    """The reference-facing entry points on the same ladder:
+    ``Simulation(ParallelTempering(Runtime(XYModel(), 128, T, seed),
+    exchange_interval=10), 0, sweeps, 10).run()`` with the reference's update
+    rule (uniform proposal, per-colour kernels), timed with CUDA events
+    around run() -- the schedule replayed as CUDA graphs, the samples
+    returned to the host.  ``host_inputs``: the initial angles and the RNG
+    streams are also copied up from host memory inside the timed region.
+    Returns (updates/ns, bytes up, bytes down)."""
+    import torch
+
+    from mcgb.core.parallel_tempering import ParallelTempering
+    from mcgb.core.runtime import Runtime
+    from mcgb.core.simulation import Simulation
+    from mcgb.models.xy.model import XYModel
+
+    rt = Runtime(XYModel(J=1.0, delta=1.5), L, temperatures(), seed=seed)
+    angles = initial_angles(seed)
+    streams = rt.rng_states.copy_to_host()
+    rt.state.copy_to_device(angles)
+    pt = ParallelTempering(rt, exchange_interval=EXCHANGE_INTERVAL)
+    Simulation(pt, 0, 2 * EXCHANGE_INTERVAL, SAMPLE_INTERVAL).run()  # loads the kernels
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    if host_inputs:
+        rt.state.copy_to_device(angles)
+        rt.rng_states.copy_to_device(streams)
+        rt.invalidate_energy_cache()
+    res = Simulation(pt, 0, sweeps, SAMPLE_INTERVAL).run()
+    e1.record()
+    torch.cuda.synchronize()
+    up = angles.nbytes + streams.nbytes if host_inputs else 0
+    down = sum(v.nbytes for v in res["samples"].values())
+    return N_TEMPS * L * L * sweeps / (e0.elapsed_time(e1) * 1e6), up, down
+
+
+def run_dropin(args, rank, world):
+    """``--api dropin``: the headline ladder through the reference's entry
+    points (see dropin_rate); one timed run of ``steps`` x 100 sweeps."""
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    if rank != 0:
+        return None
+    seed = ladder_seed(rank)
+    sweeps = args.steps * SWEEPS_PER_STEP
+    dropin_rate(max(args.warmup, 3) * SWEEPS_PER_STEP, seed)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    time.sleep(0.3)
+    value, _, _ = dropin_rate(sweeps, seed)
+    e2e, up, down = dropin_rate(sweeps, seed, host_inputs=True)
+    clk = clocks.stop()
+    return {
+        "metric": METRIC, "value": value, "unit": "updates/ns", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": N_TEMPS * L * L * SWEEPS_PER_STEP / (value * 1e6),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform angles)", "api": "dropin",
+        "config": {"workload": REFERENCE_WORKLOAD, "entry": "Simulation(ParallelTempering(Runtime(XYModel())))",
+                   "sweeps": sweeps, "exchange_interval": EXCHANGE_INTERVAL, "sample_interval": SAMPLE_INTERVAL,
+                   "l2": "inputs (2 MB angles, 8 MB streams) are L2-resident: one long run, no flush",
+                   "timed": "one Simulation.run() of all steps, samples returned to the host"},
+        "e2e": {"value": e2e, "unit": "updates/ns", "h2d_bytes_per_step": int(up / args.steps),
+                "d2h_bytes_per_step": int(down / args.steps)},
+        "clocks": clk,
+        "gpu_launches": args.steps * (SWEEPS_PER_STEP * 4 + SWEEPS_PER_STEP // EXCHANGE_INTERVAL * 4),
+    }
 
 
 def plain_fp64_rate(batch, sigma, seed):
     """The plain form (mcgb.plain64.PlainXYLadder): every replica in its own
     launches (4 colours), float64 angles, float64 Gaussian proposals and
-    exponentials, the exchange energies from a float64 reduction per lattice.
-    Times 20 sweeps with 2 exchanges."""
+    exponentials, the exchange energies from a float64 reduction per lattice,
+    each exchange interval replayed from a CUDA graph.  Times 100 sweeps with
+    10 exchanges."""
     import torch
 
     from mcgb.plain64 import PlainXYLadder
 
     ladder = PlainXYLadder(L, temperatures(), seed, sigmas=sigma.astype(np.float64),
                            exchange_interval=EXCHANGE_INTERVAL, initial_state=initial_angles(seed))
-    ladder.sweep(2)
+    ladder.sweep(2 * EXCHANGE_INTERVAL)  # captures the interval's graph
     torch.cuda.synchronize()
-    n = 20
+    n = 10 * EXCHANGE_INTERVAL
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     ladder.sweep(n)
@@ -613,8 +736,11 @@ def run_workload(args, rank, world):
     k1.record(stream)
     torch.cuda.synchronize()
     window_ms = k0.elapsed_time(k1) / 10
-    peak, peak_kind = load_peaks()
-    achieved = BYTES[kind] * n_sites * win / (window_ms * 1e-3) / 1e9
+    sm_mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    prof = PROFILE.get(args.workload)
+    roofline = roofline_line(profile_figures(prof), prof, n_sites * win, window_ms, BYTES[kind], sm_mhz,
+                             f"window_kernel ({kind})" + (f", {len(ws)} launches (size groups)" if len(ws) > 1
+                                                          else ""))
 
     # End to end: the chain state up from pinned memory, 100 sweeps, the
     # chain state and the step's samples back.
@@ -658,9 +784,7 @@ def run_workload(args, rank, world):
                    "parallelism": f"independent ladders x{world}"},
         "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": n_e2e},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": f"window_kernel ({kind})", "kernel_ms": window_ms,
-                     "bytes_per_update": BYTES[kind], "peak_source": peak_kind},
+        "roofline": roofline,
         "clocks": clk,
         "gpu_launches": args.steps * batch.launches_per_step(windows_per_step),
         "energy_drift": drift,
@@ -711,20 +835,30 @@ def profile_windows(cluster_size=4, threads=1024, workload="xy-pt-l128"):
         win = EXCHANGE_INTERVAL
     else:
         kind, ladders, ex, _, _ = workload_spec(workload)
+        fss = workload.startswith("fss-")
+        if fss:
+            # The reduced case: one ladder per size (384 replicas, an eighth
+            # of the batch), run as the bench runs it, one launch per size.
+            ladders = ladders[::8]
         seeds = [42 + L_ + 100003 * k for k, (L_, _) in enumerate(ladders)]
         inits = [seeded_state(kind, L_, len(T), sd) for (L_, T), sd in zip(ladders, seeds)]
         model = {"ising": IsingModel(), "xy": XYModel(J=1.0), "kawamura": KawamuraModel(),
                  "kawamura-gauss": KawamuraModel(), "he3": He3Model()}[kind]
+        shape = {} if fss else {"cluster_size": cluster_size, "threads": threads}
         b = LadderBatch(model, ladders, seeds=seeds, exchange_interval=ex,
                         proposal="gaussian" if kind in ("xy", "kawamura-gauss") else "uniform",
-                        gaussian=kind == "he3", cluster_size=cluster_size, threads=threads, initial_states=inits)
+                        gaussian=kind == "he3", initial_states=inits, **shape)
+        if fss:
+            b.split_by_size(True)
+            print("groups:", b.shapes())
         from mcgb.batch import NO_EXCHANGE_WINDOW
         win = ex or NO_EXCHANGE_WINDOW
-    w = b._window(win)
+    ws = [b._window(win, group=g) for g in b.groups]
     for _ in range(6):
-        _lib.call("mcgb_batch_window_run", b.model_id, ctypes.byref(w), _lib.stream_handle())
+        for w in ws:
+            _lib.call("mcgb_batch_window_run", b.model_id, ctypes.byref(w), _lib.stream_handle())
     torch.cuda.synchronize()
-    print("profile windows done")
+    print("profile windows done: %d launches per window" % len(ws))
 
 
 def main():
@@ -743,6 +877,9 @@ def main():
     ap.add_argument("--shape", default=None,
                     help="cluster_size,threads instead of autotuning (a profiler's per-launch overhead "
                          "would mislead the autotuner's timings)")
+    ap.add_argument("--api", choices=["batch", "dropin"], default="batch",
+                    help="batch: the batched engine (default); dropin: the headline ladder through "
+                         "Simulation(ParallelTempering(Runtime(XYModel())))")
     ap.add_argument("--workload", default="xy-pt-l128",
                     choices=["xy-pt-l128", "ising-l64", "kawamura-l96x64", "kawamura-l96x64-reference-proposals",
                              "he3-ragged", "fss-ising", "fss-xy"],
@@ -758,6 +895,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.api == "dropin":
+        line = run_dropin(args, rank, world)
     elif args.workload != "xy-pt-l128":
         line = run_workload(args, rank, world)
     else:

@@ -40,6 +40,8 @@ inline BatchArgs make_args(const mcgb_batch_window &w)
     a.c.first_sample_sweep = w.first_sample_sweep;
     a.c.sample_interval = w.sample_interval;
     a.c.n_sweeps = w.n_sweeps;
+    a.c.cluster_size = w.cluster_size;
+    a.c.n_clusters = w.n_clusters;
     a.state = w.state;
     a.aux = static_cast<float2 *>(w.aux);
     a.J = w.J;
@@ -137,12 +139,12 @@ inline int work_replica(const mcgb_batch_window &w, int k) { return w.host_work_
 
 // Shared memory for the largest strip among the replicas a launch runs.
 template <class M>
-inline size_t batch_smem(const mcgb_batch_window &w, int C)
+inline size_t batch_smem(const mcgb_batch_window &w, int C, bool streams = false)
 {
     size_t best = 0;
     for (int k = 0; k < work_count(w); ++k) {
         const int L = w.host_table[work_replica(w, k)].L, Ce = effective_cluster(L, C);
-        const size_t b = window_smem_bytes<M>((long long)L * L / (4 * Ce), (long long)L / 2);
+        const size_t b = window_smem_bytes<M>((long long)L * L / (4 * Ce), (long long)L / 2, streams);
         if (b > best) best = b;
     }
     return best;
@@ -159,7 +161,7 @@ template <class M, int NPMAX>
 int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t stream, const char *name)
 {
     auto kern = window_kernel<M, NPMAX>;
-    const size_t smem = batch_smem<M>(w, w.cluster_size);
+    const size_t smem = batch_smem<M>(w, w.cluster_size, smem_stream_variant<M, NPMAX>());
     MCGB_REQUIRE(smem <= 232448, "%s: a strip needs %zu bytes of shared memory (> 227 KB); use a larger "
                                  "cluster_size", name, smem);
     int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -198,6 +200,15 @@ int launch_window(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s
     return cuda_status(err, name);
 }
 
+// Whether the shared-memory stream variant fits next to a strip of `smem`
+// bytes with `threads` threads: its streams take at most 64 bytes a thread
+// (one plaquette of four colours), the bound both the variant choice and the
+// occupancy query use.
+inline bool smem_streams_fit(size_t smem, int threads)
+{
+    return smem + (size_t)64 * threads + 16 <= 232448;
+}
+
 // The variant a batch runs: the streams in registers when every strip fits,
 // preferring the two-plaquette variant (compiled for fewer threads, so with
 // the larger register budget) whenever the thread count allows it; else the
@@ -214,7 +225,9 @@ int pick_npmax(const mcgb_batch_window &w)
         if (n > npl) npl = n;
     }
     if (npl <= 2LL * w.threads && w.threads <= window_max_threads<M, 2>()) return 2;
-    if (npl <= w.threads && w.threads <= window_max_threads<M, 1>()) return 1;
+    if (npl <= w.threads && w.threads <= window_max_threads<M, 1>() &&
+        (!smem_stream_variant<M, 1>() || smem_streams_fit(batch_smem<M>(w, w.cluster_size), w.threads)))
+        return 1;
     if (M::kGlobalInFlight == 2 && w.threads <= window_max_threads<M, kGlobalPairVariant>())
         return kGlobalPairVariant;
     return 0;
@@ -238,6 +251,9 @@ template <class M, int NPMAX>
 int max_clusters_for(int C, int threads, size_t smem, int *out)
 {
     auto kern = window_kernel<M, NPMAX>;
+    // The shared-memory stream variant runs at most one plaquette a thread:
+    // its streams take at most 64 bytes a thread more.
+    if (smem_stream_variant<M, NPMAX>()) smem += (size_t)64 * threads + 16;
     int st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "cudaFuncSetAttribute(max dynamic smem)");
     if (st) return st;
@@ -268,7 +284,7 @@ int max_clusters_any(int C, int threads, size_t smem, int *out)
     MCGB_REQUIRE(threads <= M::kMaxThreads, "at most %d threads per CTA for this model", M::kMaxThreads);
     int best = 0, n = 0;
     if (int st = max_clusters_for<M, 0>(C, threads, smem, &best)) return st;
-    if (threads <= window_max_threads<M, 1>()) {
+    if (threads <= window_max_threads<M, 1>() && (!smem_stream_variant<M, 1>() || smem_streams_fit(smem, threads))) {
         if (int st = max_clusters_for<M, 1>(C, threads, smem, &n)) return st;
         if (n < best) best = n;
     }

@@ -54,6 +54,7 @@ struct KawamuraPolicy {
     static constexpr bool kPipeline = true;
     // Global-stream variant: sites whose visits one thread carries at once.
     static constexpr int kGlobalInFlight = 2;
+    static constexpr bool kSmemStreams = false;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 
@@ -436,6 +437,7 @@ struct He3Policy {
     static constexpr bool kPipeline = false;  // update<c>: one out-of-line visit
     // Global-stream variant: sites whose visits one thread carries at once.
     static constexpr int kGlobalInFlight = 1;
+    static constexpr bool kSmemStreams = false;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 

@@ -35,6 +35,8 @@ struct IsingPolicy {
     static constexpr bool kPipeline = true;
     // Global-stream variant: sites whose visits one thread carries at once.
     static constexpr int kGlobalInFlight = 2;
+    // One plaquette a thread (1024 threads): RNG streams in shared memory.
+    static constexpr bool kSmemStreams = true;
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
 
@@ -128,6 +130,8 @@ struct XYPolicy {
     static constexpr bool kPipeline = true;
     // Global-stream variant: sites whose visits one thread carries at once.
     static constexpr int kGlobalInFlight = 2;
+    // One plaquette a thread (1024 threads): RNG streams in shared memory.
+    static constexpr bool kSmemStreams = true;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
 

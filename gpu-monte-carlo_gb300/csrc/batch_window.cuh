@@ -133,6 +133,8 @@ struct WindowCommon {
     long long first_sample_sweep;
     int sample_interval;
     int n_sweeps;
+    int cluster_size;       // the launch shape the work lists were built for:
+    int n_clusters;         // a launch of another shape runs nothing (see below)
 };
 
 constexpr int kRedDoubles = 16;  // per-CTA cluster reduction slots
@@ -153,13 +155,24 @@ __host__ __device__ constexpr int part_slots()
 // window's sweeps).
 constexpr size_t kFusedCopyBytes = (sizeof(FusedExchange) + 15) & ~static_cast<size_t>(15);
 
-// Shared memory of a strip with npl plaquettes in rows of lp.
+// Shared memory of a strip with npl plaquettes in rows of lp (with
+// `streams`, also the strip's four colours of RNG streams, 16 B a site).
 template <class M>
-__host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp)
+__host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp, bool streams = false)
 {
     return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * part_slots<M>()) + kFusedCopyBytes +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
-           (size_t)4 * npl * sizeof(float) * M::kOwnFloats;
+           (size_t)4 * npl * sizeof(float) * M::kOwnFloats + (streams ? (size_t)4 * npl * 16 + 16 : 0);
+}
+
+// The one-plaquette variant (NPMAX = 1, up to 1024 threads, 64 registers)
+// of a policy with kSmemStreams keeps the strip's RNG streams in shared
+// memory instead of registers: each visit loads its stream and stores it
+// back, and the 16 registers the four streams held go to the visit.
+template <class M, int NPMAX>
+constexpr bool smem_stream_variant()
+{
+    return NPMAX == 1 && M::kSmemStreams;
 }
 
 struct StripCtx {
@@ -208,17 +221,27 @@ __device__ __forceinline__ void cluster_wait()
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
-template <class M, int NK, int C_>
+template <class M, int NK, int C_, bool SS = false>
 __device__ __forceinline__ void propose_pass(const typename M::Ctx &ctx, const typename M::Cell *cells,
                                              const float *own, const StripCtx &g, const Site (&sites)[NK],
-                                             ulonglong2 (&st)[NK][4], typename M::Prop (&prop)[NK])
+                                             ulonglong2 (&st)[NK][4], typename M::Prop (&prop)[NK],
+                                             ulonglong2 *sst = nullptr)
 {
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
         const int p = threadIdx.x + k * blockDim.x;
-        if (p < g.NPL)
-            prop[k] = M::template propose<C_>(ctx, cells[C_ * g.PS + sites[k].o + sites[k].pc],
-                                               own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, st[k][C_]);
+        if (p < g.NPL) {
+            const typename M::Cell &me = cells[C_ * g.PS + sites[k].o + sites[k].pc];
+            const float *o = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
+            if constexpr (SS) {
+                // The stream of this site, from and back to shared memory.
+                ulonglong2 v = sst[C_ * g.NPL + p];
+                prop[k] = M::template propose<C_>(ctx, me, o, v);
+                sst[C_ * g.NPL + p] = v;
+            } else {
+                prop[k] = M::template propose<C_>(ctx, me, o, st[k][C_]);
+            }
+        }
     }
 }
 
@@ -735,6 +758,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     static_assert(NS + 3 <= kRedDoubles && NS <= 32, "too many reduced sums");
     constexpr int NK = NPMAX > 0 ? NPMAX : 1;
     constexpr int GIF = NPMAX == kGlobalPairVariant ? 2 : 1;  // global variant: visits in flight
+    static_assert(!smem_stream_variant<M, NPMAX>() || M::kPipeline, "shared-memory streams need propose/decide");
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
@@ -750,6 +774,16 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     Cell *cells = reinterpret_cast<Cell *>(reinterpret_cast<unsigned char *>(fxs) + kFusedCopyBytes);
 
     const WindowCommon &cm = a.c;
+    // The work lists hold n_clusters entries for clusters of cluster_size
+    // CTAs.  A launch of any other shape -- a re-issued launch that lost its
+    // cluster attribute would run clusters of one CTA, with cluster indices
+    // far past the work lists -- touches nothing: it raises the error flag
+    // of a fused launch (the host reports it) and returns before its first
+    // memory access or barrier.  The condition is uniform over the grid.
+    if (C != cm.cluster_size || (int)gridDim.x != cm.n_clusters * cm.cluster_size) {
+        if (a.fx.enabled && blockIdx.x == 0 && tid == 0) atomicExch(a.fx.error, 1);
+        return;
+    }
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
     if (a.fx.enabled && tid == 0) *fxs = a.fx;
     // DSMEM stores below need every CTA of the cluster to be running.
@@ -772,6 +806,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         g.dn = rank + 1 >= Ce ? 0 : rank + 1;
         float *own = reinterpret_cast<float *>(
             (reinterpret_cast<uintptr_t>(cells + 4 * g.PS) + 15) & ~static_cast<uintptr_t>(15));
+        constexpr bool SS = smem_stream_variant<M, NPMAX>();
+        [[maybe_unused]] ulonglong2 *sst = reinterpret_cast<ulonglong2 *>(
+            (reinterpret_cast<uintptr_t>(own + (size_t)4 * g.NPL * M::kOwnFloats) + 15) & ~static_cast<uintptr_t>(15));
         const int64_t gplane = (int64_t)g.LP * g.LP;
         const int64_t base = rep.state_offset + (int64_t)rank * g.NPL;
 
@@ -789,7 +826,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
 
         // NPMAX > 0: the streams live in registers (the host launches this
-        // variant only when every strip fits); NPMAX = 0: global memory.
+        // variant only when every strip fits) or, for the shared-memory
+        // stream variant, in shared memory; NPMAX = 0: global memory.
         constexpr bool regs = NPMAX > 0;
         ulonglong2 st[NK][4];
         Site sites[NK];
@@ -797,11 +835,15 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         for (int k = 0; k < NK; ++k) {
             const int p = tid + k * T;
             sites[k] = make_site(p < g.NPL ? p : 0, g.LP);
-            if (regs) {
+            if (regs && !SS) {
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
                     if (p < g.NPL) st[k][c] = rng_g[base + c * gplane + p];
             }
+        }
+        if constexpr (SS) {
+            for (int c = 0; c < 4; ++c)
+                for (int p = tid; p < g.NPL; p += T) sst[c * g.NPL + p] = rng_g[base + c * gplane + p];
         }
         // A resident launch runs n_windows windows with the strip on chip,
         // exchanging between them (each walker waits for its pair's decision
@@ -865,13 +907,13 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 {
                 // Invariant: this thread has arrived at the barrier that
                 // follows the previous phase and not yet waited.
-                propose_pass<M, NK, 0>(ctx, cells, own, g, sites, st, pa);
+                propose_pass<M, NK, 0, SS>(ctx, cells, own, g, sites, st, pa, sst);
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
                 decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 cluster_arrive();
-                propose_pass<M, NK, 1>(ctx, cells, own, g, sites, st, pa);
-                propose_pass<M, NK, 2>(ctx, cells, own, g, sites, st, pb);
+                propose_pass<M, NK, 1, SS>(ctx, cells, own, g, sites, st, pa, sst);
+                propose_pass<M, NK, 2, SS>(ctx, cells, own, g, sites, st, pb, sst);
                 cluster_wait();
                 decide_pass<M, NK, 1>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 if (M::kSplitMiddle) {
@@ -880,7 +922,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 }
                 decide_pass<M, NK, 2>(ctx, cells, own, g, sites, pb, dacc, nacc);
                 cluster_arrive();
-                propose_pass<M, NK, 3>(ctx, cells, own, g, sites, st, pa);
+                propose_pass<M, NK, 3, SS>(ctx, cells, own, g, sites, st, pa, sst);
                 cluster_wait();
                 decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 }
@@ -954,7 +996,10 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 M::store(a, base + c * gplane + p, cells[c * g.PS + s.o + s.pc],
                          own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
             }
-        if (regs) {
+        if constexpr (SS) {
+            for (int c = 0; c < 4; ++c)
+                for (int p = tid; p < g.NPL; p += T) rng_g[base + c * gplane + p] = sst[c * g.NPL + p];
+        } else if (regs) {
 #pragma unroll
             for (int k = 0; k < NK; ++k) {
                 const int p = tid + k * T;

@@ -252,6 +252,33 @@ __global__ void xy64_energy_kernel(const double *__restrict__ theta, int L, int 
     if (threadIdx.x == 0) out[r] = v[0];
 }
 
+// The five channels of models/xy/measure.py:17-134 (energy, mx, my,
+// twist_cos_x, twist_sin_x) of lattice r of the plain float64 form, into
+// column w2t[r] (or r) of out (5, n_out).
+__global__ void xy64_measure_kernel(const double *__restrict__ theta, int L, int r, double J,
+                                    const int32_t *__restrict__ w2t, double *__restrict__ out, int n_out)
+{
+    __shared__ double scratch[32 * 5];
+    const double *b = theta + (int64_t)r * L * L;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
+        const int i = k / L, j = k - i * L;
+        const double t = b[k];
+        const double dx = t - b[wrapi(i + 1, L) * L + j];
+        const double cx = cos(dx);
+        v[0] += -J * (cx + cos(t - b[i * L + wrapi(j + 1, L)]));
+        v[1] += cos(t);
+        v[2] += sin(t);
+        v[3] += cx;
+        v[4] += sin(dx);
+    }
+    block_sum<5>(v, scratch);
+    if (threadIdx.x == 0) {
+        const int col = w2t != nullptr ? w2t[r] : r;
+        for (int c = 0; c < 5; ++c) out[(int64_t)c * n_out + col] = v[c];
+    }
+}
+
 // ============================================================== Kawamura
 // models/kawamura/update.py:7-65
 
@@ -501,6 +528,16 @@ extern "C" int mcgb_xy64_energy(const double *theta, int R, int L, int r, double
     MCGB_REQUIRE(r >= 0 && r < R, "xy64_energy: replica out of range");
     xy64_energy_kernel<<<1, 1024, 0, as_stream(stream)>>>(theta, L, r, J, out);
     return check_launch("xy64_energy_kernel");
+}
+
+extern "C" int mcgb_xy64_measure(const double *theta, int R, int L, int r, double J, const int32_t *w2t,
+                                  double *out, void *stream)
+{
+    if (int st = check_lattice("xy64_measure", R, L)) return st;
+    MCGB_REQUIRE(theta && out, "xy64_measure: null pointer");
+    MCGB_REQUIRE(r >= 0 && r < R, "xy64_measure: replica out of range");
+    xy64_measure_kernel<<<1, 1024, 0, as_stream(stream)>>>(theta, L, r, J, w2t, out, R);
+    return check_launch("xy64_measure_kernel");
 }
 
 extern "C" int mcgb_xy_energy(const float *theta, int R, int L, float J, double *out, void *stream)

@@ -33,6 +33,7 @@ SIGNATURES = {
     "mcgb_xy_update_color_gauss": [_P, _P, _P, _P, _I, _I, _I, _F, _P],
     "mcgb_xy64_update_color": [_P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _P],
     "mcgb_xy64_energy": [_P, _I, _I, _I, _D, _P, _P],
+    "mcgb_xy64_measure": [_P, _I, _I, _I, _D, _P, _P, _P],
     "mcgb_xy_energy": [_P, _I, _I, _F, _P, _P],
     "mcgb_xy_measure": [_P, _I, _I, _F, _P, _P, _P, _P],
     "mcgb_kawamura_update_color": [_P, _P, _P, _I, _I, _I, _F, _F, _P],
@@ -46,6 +47,9 @@ SIGNATURES = {
     "mcgb_he3_local_differences": [_P, _I, _I, _P, _P, _I, _P, _F, _F, _P, _P],
     "mcgb_pt_exchange": [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I64, _P],
     "mcgb_pt_record_walkers": [_P, _P, _P, _I, _P],
+    "mcgb_pt_exchange_clocked": [_P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _P],
+    "mcgb_pt_record_walkers_ring": [_P, _P, _P, _P, _I, _I64, _P],
+    "mcgb_ring_push": [_P, _P, _P, _I64, _I64, _P],
     "mcgb_batch_channels": [_I],
     "mcgb_batch_smem_bytes": [_I, _I, _I],
     "mcgb_batch_max_clusters": [_I, _I, _I, _I64, _P],

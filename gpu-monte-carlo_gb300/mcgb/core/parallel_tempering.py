@@ -172,6 +172,45 @@ class ParallelTempering:
                 and self.exchange_rounds % self._history_stride == 0):
             self._record_walker_history()
 
+    # ------------------------------------------------------------ replay hooks
+    # Simulation replays whole schedules as captured CUDA graphs: these
+    # enqueue the device work of one exchange round with the schedule read
+    # from a device clock {sweeps, rounds}, and account on the host for the
+    # rounds a replay ran.
+
+    def _enqueue_exchange(self, clock, advance):
+        """attempt_exchanges' launches: fresh energies, then the round after
+        clock[0] + advance sweeps at parity clock[1] % 2 (no host state)."""
+        rt = self.runtime
+        rt.model.measure_energy(rt.state, self.energies)
+        _lib.call("mcgb_pt_exchange_clocked", ptr(self.energies), ptr(rt.betas),
+                  ptr(self.walker_to_temperature), ptr(self.temperature_to_walker),
+                  ptr(self._rng_states), ptr(self._swap_counts), ptr(self._trips),
+                  self.R, ptr(clock), int(advance), _lib.stream_handle())
+
+    def _enqueue_history(self, ring, head):
+        """A walker-history row into the device ring ``ring[head]``."""
+        _lib.call("mcgb_pt_record_walkers_ring", ptr(self.walker_to_temperature),
+                  ptr(self._tracked_walkers_gpu), ptr(ring), ptr(head), len(self._tracked_walkers),
+                  int(ring.shape[0]), _lib.stream_handle())
+
+    def _rounds_done(self, sweeps, rounds, history=None, coordinates=()):
+        """Host bookkeeping after a replay that ran ``sweeps`` sweeps and
+        ``rounds`` exchange rounds; ``history`` holds the walker-history rows
+        it recorded at the (sweep, round) ``coordinates``."""
+        self.sweeps += sweeps
+        self.exchange_rounds += rounds
+        if self.R > 2 and rounds % 2:
+            self._parity = 1 - self._parity
+        for k, (sweep, rnd) in enumerate(coordinates):
+            row = len(self._history_sweeps) % self._history_chunk_rows
+            if row == 0:
+                self._history_chunks.append(device_array(
+                    (self._history_chunk_rows, len(self._tracked_walkers)), dtype=np.int32))
+            self._history_chunks[-1][row].raw().copy_(history[k].raw())
+            self._history_sweeps.append(sweep)
+            self._history_rounds.append(rnd)
+
     def measure(self):
         """CPU observables in the fixed temperature order."""
         return self.runtime.measure(temperature_indices=self.walker_to_temperature)

@@ -41,8 +41,15 @@ class OutputBuffer:
         return self._buf
 
 
-def measure_call(fn_name, out, names, *args):
+def launch_measure(fn_name, out, channels, R, who, *args):
+    """Enqueue a (channels, R) float64 measurement into the device array ``out``."""
+    if tuple(out.shape) != (channels, R) or np.dtype(out.dtype) != np.float64:
+        raise ValueError(f"{who}: output must be a float64 device array of shape ({channels}, {R})")
     _lib.call(fn_name, *args, ptr(out), _lib.stream_handle())
+
+
+def read_channels(out, names):
+    """Copy a (channels, R) measurement to the host as {name: (R,) array}."""
     values = out.copy_to_host()
     return {name: values[c].copy() for c, name in enumerate(names)}
 

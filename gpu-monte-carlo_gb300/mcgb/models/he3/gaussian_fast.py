@@ -30,14 +30,18 @@ class FastGaussianUpdater:
         self.sweeps = 0
 
     def step(self):
+        self.runtime.invalidate_energy_cache()
+        self.enqueue()
+        self.sweeps += 1
+
+    def enqueue(self):
+        """The four colour launches of one sweep, nothing on the host."""
         rt = self.runtime
-        rt.invalidate_energy_cache()
         model = rt.model
         for color in range(4):
             _lib.call("mcgb_he3_gaussian_update_color", ptr(rt.state), ptr(rt.rng_states), ptr(rt.betas),
                       rt.R, rt.L, color, model._cptr(), float(model.K), float(self.rho), float(self.mass),
                       float(model.g_d), ptr(self.counts), _lib.stream_handle())
-        self.sweeps += 1
 
     def diagnostics(self):
         counts = self.counts.copy_to_host().sum(axis=(2, 3))

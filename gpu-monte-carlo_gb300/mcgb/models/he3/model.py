@@ -13,7 +13,7 @@ import numpy as np
 from ... import _lib
 from ...core.model import Model
 from ...device import device_array, ptr, to_device
-from .._common import (OutputBuffer, check_rng, check_vector, geometry, measure_call,
+from .._common import (OutputBuffer, check_rng, check_vector, geometry, launch_measure, read_channels,
                        optional_cache, optional_indices)
 
 MEASUREMENT_NAMES = (
@@ -85,13 +85,23 @@ class He3Model(Model):
         _lib.call("mcgb_he3_update_color", ptr(state), ptr(rng_states), ptr(betas), R, L, int(color),
                   self._cptr(), float(self.K), float(self.delta), float(self.g_d), _lib.stream_handle())
 
-    def measure(self, state, temperature_indices=None, cached_energies=None):
+    measurement_names = MEASUREMENT_NAMES
+
+    def measure_into(self, state, out, temperature_indices=None, cached_energies=None):
+        """Enqueue the measurement into the (channels, R) float64 device array
+        ``out`` without copying it to the host (the device sample ring of
+        Simulation uses this)."""
         R, L = geometry(state, np.complex64, (3, 2), "He3Model.measure")
+        launch_measure("mcgb_he3_measure", out, len(MEASUREMENT_NAMES), R, "He3Model.measure", ptr(state), R, L,
+                       self._cptr(), float(self.K), float(self.g_d),
+                       optional_indices(temperature_indices, R, "He3Model.measure"),
+                       optional_cache(cached_energies, R, "He3Model.measure"))
+
+    def measure(self, state, temperature_indices=None, cached_energies=None):
+        R = int(state.shape[0])
         out = self._out.get(len(MEASUREMENT_NAMES), R)
-        return measure_call("mcgb_he3_measure", out, MEASUREMENT_NAMES, ptr(state), R, L, self._cptr(),
-                            float(self.K), float(self.g_d),
-                            optional_indices(temperature_indices, R, "He3Model.measure"),
-                            optional_cache(cached_energies, R, "He3Model.measure"))
+        self.measure_into(state, out, temperature_indices, cached_energies)
+        return read_channels(out, MEASUREMENT_NAMES)
 
     def measure_with_energy(self, state, energies, temperature_indices=None):
         return self.measure(state, temperature_indices=temperature_indices, cached_energies=energies)

@@ -19,5 +19,11 @@ class He3GaussianRuntime(Runtime):
     def sweep(self):
         self.gaussian.step()
 
+    def _enqueue_sweep(self):
+        self.gaussian.enqueue()
+
+    def _sweeps_done(self, n):
+        self.gaussian.sweeps += n
+
     def sampling_diagnostics(self):
         return self.gaussian.diagnostics()

@@ -13,7 +13,7 @@ import numpy as np
 from ... import _lib
 from ...core.model import Model
 from ...device import ptr
-from .._common import (OutputBuffer, check_rng, check_vector, geometry, measure_call,
+from .._common import (OutputBuffer, check_rng, check_vector, geometry, launch_measure, read_channels,
                        optional_cache, optional_indices)
 
 MEASUREMENT_NAMES = ("energy", "chirality", "px", "py", "spin2", "twist_cos_x", "twist_sin_x")
@@ -39,12 +39,22 @@ class KawamuraModel(Model):
         _lib.call("mcgb_kawamura_update_color", ptr(state), ptr(rng_states), ptr(betas), R, L,
                   int(color), float(self.J), float(self.delta), _lib.stream_handle())
 
-    def measure(self, state, temperature_indices=None, cached_energies=None):
+    measurement_names = MEASUREMENT_NAMES
+
+    def measure_into(self, state, out, temperature_indices=None, cached_energies=None):
+        """Enqueue the measurement into the (channels, R) float64 device array
+        ``out`` without copying it to the host (the device sample ring of
+        Simulation uses this)."""
         R, L = geometry(state, np.float32, (5,), "KawamuraModel.measure")
+        launch_measure("mcgb_kawamura_measure", out, len(MEASUREMENT_NAMES), R, "KawamuraModel.measure", ptr(state), R, L,
+                       float(self.J), optional_indices(temperature_indices, R, "KawamuraModel.measure"),
+                       optional_cache(cached_energies, R, "KawamuraModel.measure"))
+
+    def measure(self, state, temperature_indices=None, cached_energies=None):
+        R = int(state.shape[0])
         out = self._out.get(len(MEASUREMENT_NAMES), R)
-        return measure_call("mcgb_kawamura_measure", out, MEASUREMENT_NAMES, ptr(state), R, L,
-                            float(self.J), optional_indices(temperature_indices, R, "KawamuraModel.measure"),
-                            optional_cache(cached_energies, R, "KawamuraModel.measure"))
+        self.measure_into(state, out, temperature_indices, cached_energies)
+        return read_channels(out, MEASUREMENT_NAMES)
 
     def measure_with_energy(self, state, energies, temperature_indices=None):
         return self.measure(state, temperature_indices=temperature_indices, cached_energies=energies)

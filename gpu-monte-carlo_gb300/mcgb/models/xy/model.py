@@ -14,7 +14,7 @@ import numpy as np
 from ... import _lib
 from ...core.model import Model
 from ...device import ptr
-from .._common import (OutputBuffer, check_rng, check_vector, geometry, measure_call,
+from .._common import (OutputBuffer, check_rng, check_vector, geometry, launch_measure, read_channels,
                        optional_cache, optional_indices)
 
 MEASUREMENT_NAMES = ("energy", "mx", "my", "twist_cos_x", "twist_sin_x")
@@ -52,12 +52,22 @@ class XYModel(Model):
             _lib.call("mcgb_xy_update_color_gauss", ptr(state), ptr(rng_states), ptr(betas),
                       ptr(self.sigmas), R, L, int(color), float(self.J), _lib.stream_handle())
 
-    def measure(self, state, temperature_indices=None, cached_energies=None):
+    measurement_names = MEASUREMENT_NAMES
+
+    def measure_into(self, state, out, temperature_indices=None, cached_energies=None):
+        """Enqueue the measurement into the (channels, R) float64 device array
+        ``out`` without copying it to the host (the device sample ring of
+        Simulation uses this)."""
         R, L = geometry(state, np.float32, (), "XYModel.measure")
+        launch_measure("mcgb_xy_measure", out, len(MEASUREMENT_NAMES), R, "XYModel.measure", ptr(state), R, L,
+                       float(self.J), optional_indices(temperature_indices, R, "XYModel.measure"),
+                       optional_cache(cached_energies, R, "XYModel.measure"))
+
+    def measure(self, state, temperature_indices=None, cached_energies=None):
+        R = int(state.shape[0])
         out = self._out.get(len(MEASUREMENT_NAMES), R)
-        return measure_call("mcgb_xy_measure", out, MEASUREMENT_NAMES, ptr(state), R, L, float(self.J),
-                            optional_indices(temperature_indices, R, "XYModel.measure"),
-                            optional_cache(cached_energies, R, "XYModel.measure"))
+        self.measure_into(state, out, temperature_indices, cached_energies)
+        return read_channels(out, MEASUREMENT_NAMES)
 
     def measure_with_energy(self, state, energies, temperature_indices=None):
         return self.measure(state, temperature_indices=temperature_indices, cached_energies=energies)

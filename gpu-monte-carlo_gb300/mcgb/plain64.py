@@ -11,14 +11,21 @@ pair parity.
 
 This is the baseline the mixed-precision batched engine is compared with:
 the same Markov chain family, computed the plain way.  Nothing in the batched
-engine depends on it.
+engine depends on it.  ``sweep`` replays each full exchange interval (its
+per-lattice launches and the exchange) from a captured CUDA graph, with the
+exchange's sweep and parity read from a device clock, so the form is timed
+by its kernels -- one lattice per launch, float64 arithmetic -- and not by
+host dispatch; ``graph=False`` launches everything directly.
 """
 
 import numpy as np
+import torch
 
 from . import _lib
 from .device import device_zeros, to_device
 from .rng import create_xoroshiro128p_states
+
+CHANNELS = ("energy", "mx", "my", "twist_cos_x", "twist_sin_x")
 
 
 class PlainXYLadder:
@@ -69,37 +76,82 @@ class PlainXYLadder:
         self.sweeps = 0
         self.exchange_rounds = 0
         self._parity = 0
+        # Device clock {sweeps at the last exchange, rounds} read by the
+        # clocked exchange kernel; sweeps since then, on the host.
+        self.clock = device_zeros(2, np.int64)
+        self._since_exchange = 0
+        self._graphs = {}
+        self._measured = device_zeros((len(CHANNELS), self.R), np.float64)
 
     def _energy(self, s):
         for r in range(self.R):
             _lib.call("mcgb_xy64_energy", self.theta.cptr, self.R, self.L, r, self.J, self.energies.cptr, s)
 
-    def sweep(self, n=1):
+    def _enqueue(self, n_sweeps, exchange, advance):
+        """Launches of n_sweeps sweeps and, if `exchange`, of the exchange
+        round ``advance`` sweeps after the previous one (no host state)."""
         s = _lib.stream_handle()
         sig = None if self.sigmas is None else self.sigmas.cptr
-        for _ in range(int(n)):
+        for _ in range(n_sweeps):
             for r in range(self.R):
                 for c in range(4):
                     _lib.call("mcgb_xy64_update_color", self.theta.cptr, self.rng.cptr, self.betas64.cptr, sig,
                               self.w2t.cptr, self.R, self.L, r, c, self.J, self.delta, s)
-            self.sweeps += 1
-            if self.sweeps % self.exchange_interval == 0:
-                self._energy(s)
-                _lib.call("mcgb_pt_exchange", self.energies.cptr, self.betas32.cptr, self.w2t.cptr,
-                          self.t2w.cptr, self.exchange_rng.cptr, self.swap_counts.cptr, self.trips.cptr,
-                          self.R, self._parity, self.sweeps, s)
+        if exchange:
+            self._energy(s)
+            _lib.call("mcgb_pt_exchange_clocked", self.energies.cptr, self.betas32.cptr, self.w2t.cptr,
+                      self.t2w.cptr, self.exchange_rng.cptr, self.swap_counts.cptr, self.trips.cptr,
+                      self.R, self.clock.cptr, int(advance), s)
+
+    def sweep(self, n=1, graph=True):
+        """n sweeps with an exchange attempt every ``exchange_interval``
+        sweeps (ParallelTempering.sweep's schedule, alternating parity)."""
+        left = int(n)
+        while left > 0:
+            to_exchange = self.exchange_interval - self.sweeps % self.exchange_interval
+            k = min(left, to_exchange)
+            exchange = k == to_exchange
+            advance = self._since_exchange + k
+            if graph and exchange and k == self.exchange_interval:
+                # A whole interval in this call (so advance == k): one graph.
+                g = self._graphs.get(k)
+                if g is None:
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g):
+                        self._enqueue(k, True, k)
+                    self._graphs[k] = g
+                g.replay()
+            else:
+                self._enqueue(k, exchange, advance)
+            self.sweeps += k
+            left -= k
+            if exchange:
+                self._since_exchange = 0
                 self.exchange_rounds += 1
                 if self.R > 2:
                     self._parity = 1 - self._parity
+            else:
+                self._since_exchange = advance
 
     def measure_energy(self):
         """Float64 total energies in temperature order."""
         self._energy(_lib.stream_handle())
         return self.energies.copy_to_host()[self.t2w.copy_to_host()]
 
-    def simulate(self, thermalization_sweeps=1000, measurement_sweeps=4000, sample_interval=10):
-        """The Simulation.run schedule (core/simulation.py:28-96) with the energy
-        as the one channel: ``{"samples": {"energy": (n, R)}, "metadata": ...}``."""
+    def measure(self):
+        """The reference's five XY channels (models/xy/measure.py:17-134),
+        summed in float64, in temperature order: {name: (R,)}."""
+        s = _lib.stream_handle()
+        for r in range(self.R):
+            _lib.call("mcgb_xy64_measure", self.theta.cptr, self.R, self.L, r, self.J, self.w2t.cptr,
+                      self._measured.cptr, s)
+        values = self._measured.copy_to_host()
+        return {name: values[c].copy() for c, name in enumerate(CHANNELS)}
+
+    def simulate(self, thermalization_sweeps=1000, measurement_sweeps=4000, sample_interval=10, channels="all"):
+        """The Simulation.run schedule (core/simulation.py:28-96):
+        ``{"samples": {channel: (n, R)}, "metadata": ...}`` with the five XY
+        channels (``channels="energy"``: the energy alone)."""
         if thermalization_sweeps < 0:
             raise ValueError("Thermalization sweeps cannot be negative")
         if measurement_sweeps < 1:
@@ -111,7 +163,7 @@ class PlainXYLadder:
         for k in range(1, measurement_sweeps + 1):
             self.sweep(1)
             if k % sample_interval == 0:
-                rows.append(self.measure_energy())
+                rows.append(self.measure() if channels == "all" else {"energy": self.measure_energy()})
         counts = self.swap_counts.copy_to_host()
         metadata = {"L": self.L, "temperatures": self.temperatures.copy(),
                     "model_parameters": {"J": self.J, "delta": self.delta},
@@ -119,4 +171,4 @@ class PlainXYLadder:
                     "sample_interval": sample_interval,
                     "acceptance_rates": np.divide(counts[1], counts[0], out=np.zeros(self.R - 1),
                                                   where=counts[0] > 0)}
-        return {"samples": {"energy": np.stack(rows)}, "metadata": metadata}
+        return {"samples": {k: np.stack([row[k] for row in rows]) for k in rows[0]}, "metadata": metadata}

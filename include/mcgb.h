@@ -97,6 +97,11 @@ int mcgb_xy64_update_color(double *theta, void *rng, const double *betas,
 /* FP64 energy of one lattice (replica r) into out[r]. */
 int mcgb_xy64_energy(const double *theta, int R, int L, int r, double J, double *out,
                      void *stream);
+/* The five channels of models/xy/measure.py:17-101 (energy, mx, my,
+ * twist_cos_x, twist_sin_x) of one lattice of the plain FP64 form, summed in
+ * float64, into column w2t[r] (w2t NULL: r) of out (5, R). */
+int mcgb_xy64_measure(const double *theta, int R, int L, int r, double J, const int32_t *w2t,
+                      double *out, void *stream);
 /* models/xy/measure.py:104-134 xy_energy_kernel. */
 int mcgb_xy_energy(const float *theta, int R, int L, float J, double *out, void *stream);
 /* models/xy/measure.py:17-101: out (5, R) = energy, mx, my, twist_cos_x,
@@ -165,6 +170,28 @@ int mcgb_pt_exchange(const double *energies, float *betas, int32_t *walker_to_te
  * history_row[k] = walker_to_temperature[walker_ids[k]]. */
 int mcgb_pt_record_walkers(const int32_t *walker_to_temperature, const int32_t *walker_ids,
                            int32_t *history_row, int n, void *stream);
+/* core/parallel_tempering.py:35-91 _exchange_kernel with the schedule
+ * arguments it takes from ParallelTempering.attempt_exchanges
+ * (core/parallel_tempering.py:255-269: `self._parity`, `self.sweeps`) read
+ * from a device clock int64 {sweeps, rounds} instead: the round runs after
+ * clock[0] + advance sweeps at parity rounds % 2 (0 when R == 2), then the
+ * clock becomes {clock[0] + advance, rounds + 1}.  Same results as
+ * mcgb_pt_exchange; a captured CUDA graph of it replays each round at its
+ * own sweep and parity. */
+int mcgb_pt_exchange_clocked(const double *energies, float *betas, int32_t *walker_to_temperature,
+                             int32_t *temperature_to_walker, void *rng, int64_t *swap_counts,
+                             int64_t *trips, int R, int64_t *clock, int advance, void *stream);
+/* core/parallel_tempering.py:206-216 _record_walker_history into a device
+ * ring: row head[0] % capacity of ring [capacity][n] receives
+ * walker_to_temperature[walker_ids[k]], then head[0] += 1 (replaces the
+ * per-row pointer of mcgb_pt_record_walkers inside captured graphs). */
+int mcgb_pt_record_walkers_ring(const int32_t *walker_to_temperature, const int32_t *walker_ids,
+                                int32_t *ring, int64_t *head, int n, int64_t capacity, void *stream);
+/* core/simulation.py:39-66 sample accumulation (`samples[name].append`)
+ * on the device: copy n float64 values from src to slot head[0] % capacity
+ * of ring [capacity][n], then head[0] += 1.  One bulk copy of the ring
+ * replaces a host copy per sample. */
+int mcgb_ring_push(const double *src, double *ring, int64_t *head, int64_t n, int64_t capacity, void *stream);
 
 /* ------------------------------------------------------------ Handle API
  * One reference Runtime (core/runtime.py:8-135) with its ParallelTempering

@@ -36,19 +36,64 @@ def jackknife(moments, estimator, block_size):
 
 
 def xy_observables(samples, L, temperatures, J=1.0, block_size=100):
-    """Energy per site, Binder cumulant 1 - <m^4>/(2<m^2>^2), helicity modulus."""
+    """Energy per site, Binder cumulant 1 - <m^4>/(2<m^2>^2), helicity
+    modulus (models/xy/analysis.py:47-54) and <|m|> per site."""
     T = np.asarray(temperatures, dtype=np.float64)
     m2 = np.asarray(samples["mx"]) ** 2 + np.asarray(samples["my"]) ** 2
     qx = np.asarray(samples["twist_sin_x"], dtype=np.float64)
     moments = {"e": np.asarray(samples["energy"]) / L ** 2, "m2": m2, "m4": m2 ** 2,
-               "cx": np.asarray(samples["twist_cos_x"]), "qx": qx, "qx2": qx ** 2}
+               "cx": np.asarray(samples["twist_cos_x"]), "qx": qx, "qx2": qx ** 2,
+               "absm": np.sqrt(m2) / L ** 2}
 
     def est(m):
         helicity = (J * m["cx"] - J ** 2 / T * (m["qx2"] - m["qx"] ** 2)) / L ** 2
-        return np.stack((m["e"], 1 - m["m4"] / (2 * m["m2"] ** 2), helicity))
+        return np.stack((m["e"], 1 - m["m4"] / (2 * m["m2"] ** 2), helicity, m["absm"]))
 
     value, error = jackknife(moments, est, block_size)
-    return dict(zip(("energy", "binder", "helicity"), zip(value, error)))
+    return dict(zip(("energy", "binder", "helicity", "magnetization"), zip(value, error)))
+
+
+def linear_crossings(T, y1, y2):
+    """Temperatures where two piecewise-linear curves cross (the method of
+    utils/Analysis/crossings.py:5-24): sample points where they agree and
+    linear interpolation inside every sign change of y1 - y2."""
+    T = np.asarray(T, dtype=np.float64)
+    d = np.asarray(y1, dtype=np.float64) - np.asarray(y2, dtype=np.float64)
+    if not np.all(np.isfinite(d)) or np.any((d[:-1] == 0) & (d[1:] == 0)):
+        return []
+    roots = list(T[d == 0])
+    for i in np.where(d[:-1] * d[1:] < 0)[0]:
+        roots.append(T[i] - d[i] * (T[i + 1] - T[i]) / (d[i + 1] - d[i]))
+    return sorted(float(t) for t in roots)
+
+
+def binder_crossing(samples_a, samples_b, temperatures, binder, block_size):
+    """The unique crossing of two sizes' Binder curves with its block
+    jackknife error, or None when the full-sample curves do not cross once
+    (``binder(moments) -> curve`` maps block means of the "m2", "m4" moments
+    to the Binder curve)."""
+    def moments(samples):
+        m2 = np.asarray(samples["m2"], np.float64)
+        return {"m2": m2, "m4": m2 ** 2}
+    ma, mb = moments(samples_a), moments(samples_b)
+    ba = {k: blocks_of(v, block_size) for k, v in ma.items()}
+    bb = {k: blocks_of(v, block_size) for k, v in mb.items()}
+    B = min(len(ba["m2"]), len(bb["m2"]))
+    ta = {k: v[:B].sum(0) for k, v in ba.items()}
+    tb = {k: v[:B].sum(0) for k, v in bb.items()}
+    full = linear_crossings(temperatures, binder({k: v / B for k, v in ta.items()}),
+                            binder({k: v / B for k, v in tb.items()}))
+    if len(full) != 1:
+        return None
+    est = []
+    for b in range(B):
+        c = linear_crossings(temperatures, binder({k: (ta[k] - ba[k][b]) / (B - 1) for k in ta}),
+                             binder({k: (tb[k] - bb[k][b]) / (B - 1) for k in tb}))
+        est.append(c[0] if len(c) == 1 else np.nan)
+    est = np.asarray(est)
+    if not np.all(np.isfinite(est)):
+        return None
+    return full[0], float(np.sqrt((B - 1) / B * ((est - est.mean()) ** 2).sum()))
 
 
 def energy_observable(samples, L, block_size=100):

@@ -53,3 +53,28 @@ def test_family_bound_reproduces_the_single_test_rate():
     # 18 comparisons at a 0.27 % family-wise rate: 3.79 sigma each.
     assert stats.family_bound(18) == pytest.approx(3.791, abs=0.001)
     assert stats.family_bound(28) > stats.family_bound(18)
+
+
+def test_linear_crossings_follow_the_reference_rules():
+    T = np.array([1.0, 2.0, 3.0, 4.0])
+    assert stats.linear_crossings(T, [0, 1, 2, 3], [3, 2, 1, 0]) == [2.5]
+    assert stats.linear_crossings(T, [1, 2, 2, 4], [0, 2, 3, 3]) == [2.0, 3.5]
+    assert stats.linear_crossings(T, [1, 1, 2, 3], [1, 1, 0, 0]) == []   # an interval of roots
+    assert stats.linear_crossings(T, [1, 2, 3, 4], [0, 0, 0, 0]) == []
+
+
+def test_binder_crossing_recovers_a_planted_crossing():
+    # m2 = 1 + s z^2 (z normal) has Binder value 1 - (1 + 2s + 3s^2) / (2 (1 + s)^2),
+    # monotonic in s; s_a(T) and s_b(T) are equal at T = 1.5 only.
+    r = np.random.default_rng(3)
+    T = np.linspace(1.0, 2.0, 11)
+    n = 20000
+
+    def fake(slope):
+        scale = np.exp(slope * (T - 1.5))
+        return {"m2": 1 + scale * r.normal(size=(n, T.size)) ** 2}
+    binder = (lambda m: 1 - m["m4"] / (2 * m["m2"] ** 2))
+    got = stats.binder_crossing(fake(1.0), fake(-1.0), T, binder, block_size=1000)
+    assert got is not None
+    value, err = got
+    assert 0 < err < 0.05 and abs(value - 1.5) < 4 * err
