@@ -97,18 +97,23 @@ def profile_figures(name):
     return out
 
 
-def roofline_line(figs, source, updates_per_launch, launch_ms, bytes_per_update, sm_mhz, kernel):
-    """The window kernel against the bound that binds it, instruction issue.
+def roofline_line(figs, source, updates_per_launch, launch_ms, bytes_per_update, sm_mhz, kernel,
+                  scale_traffic=False):
+    """The window kernel against the bound that binds it.
 
-    achieved = warp instructions per launch / the launch's event-timed
-    duration, where warp instructions per attempted update come from the ncu
-    capture (smsp__inst_executed.sum over the updates of the captured
-    launch); peak = SMs x 4 schedulers x 1 warp instruction per cycle x the
-    SM clock sampled during the timed region.  The algorithmic-HBM figure
-    (bytes per update x updates / duration, against the measured copy
-    bandwidth) rides along under "hbm": the kernel keeps state and streams on
-    chip, so its DRAM traffic ("traffic", per launch, from the same capture)
-    is a small fraction of the algorithmic bytes."""
+    Two bounds are evaluated.  Instruction issue: warp instructions per
+    launch (per attempted update from the ncu capture, smsp__inst_executed.sum
+    over the captured launch's updates) / the launch's event-timed duration,
+    against SMs x 4 schedulers x 1 warp instruction per cycle x the SM clock
+    sampled during the timed region.  HBM: the capture's DRAM bytes
+    (dram__bytes_read.sum + write.sum, per launch; with ``scale_traffic``
+    scaled from the captured case to this launch by the updates each
+    processes) over the duration, against the measured copy bandwidth.  The
+    larger fraction names the bound.  With "issue", "achieved"/"peak" are
+    warp instructions per second; with "hbm" they are the model's
+    algorithmic bytes (state r+w + 32 B of RNG stream per update) per
+    second, as the roofline of a bandwidth-bound kernel counts them; both
+    figures appear under "issue" and "hbm"."""
     import torch
     peak_hbm, peak_kind = load_peaks()
     alg = bytes_per_update * updates_per_launch / (launch_ms * 1e-3) / 1e9
@@ -117,19 +122,27 @@ def roofline_line(figs, source, updates_per_launch, launch_ms, bytes_per_update,
     traffic = None
     if "dram__bytes_read.sum" in figs and "dram__bytes_write.sum" in figs:
         traffic = figs["dram__bytes_read.sum"] + figs["dram__bytes_write.sum"]
-    line = {"bound": "issue", "achieved": None, "peak": issue_peak, "unit": "G warp-instructions/s",
-            "frac": None, "traffic": traffic, "kernel": kernel, "kernel_ms": launch_ms,
-            "peak_source": f"{n_sm} SMs x 4 schedulers x {sm_mhz:.0f} MHz (sampled)",
-            "hbm": {"achieved": alg, "peak": peak_hbm, "unit": "GB/s", "frac": alg / peak_hbm,
-                    "bytes_per_update": bytes_per_update, "peak_source": peak_kind,
-                    "note": "algorithmic bytes (state r+w + 32 B of RNG stream per update) over the "
-                            "kernel time; the kernel keeps them on chip, see traffic"},
-            "source": f"profiles/{source}" if figs else None}
+        if scale_traffic and figs.get("updates"):
+            traffic *= updates_per_launch / figs["updates"]
+    dram_frac = None if traffic is None else traffic / (launch_ms * 1e-3) / 1e9 / peak_hbm
+    hbm = {"achieved": alg, "peak": peak_hbm, "unit": "GB/s", "frac": alg / peak_hbm,
+           "bytes_per_update": bytes_per_update, "peak_source": peak_kind,
+           "dram_frac": dram_frac,
+           "note": "achieved: algorithmic bytes (state r+w + 32 B of RNG stream per update) over the kernel time; "
+                   "dram_frac: the DRAM bytes actually moved (traffic) over the kernel time"}
+    issue = {"achieved": None, "peak": issue_peak, "unit": "G warp-instructions/s", "frac": None,
+             "peak_source": f"{n_sm} SMs x 4 schedulers x {sm_mhz:.0f} MHz (sampled)"}
     if "smsp__inst_executed.sum" in figs and figs.get("updates"):
         per_update = figs["smsp__inst_executed.sum"] / figs["updates"]
         achieved = per_update * updates_per_launch / (launch_ms * 1e-3) / 1e9
-        line.update({"achieved": achieved, "frac": achieved / issue_peak,
-                     "warp_instructions_per_update": per_update})
+        issue.update({"achieved": achieved, "frac": achieved / issue_peak, "warp_instructions_per_update": per_update})
+    line = {"traffic": traffic, "kernel": kernel, "kernel_ms": launch_ms, "issue": issue, "hbm": hbm,
+            "source": f"profiles/{source}" if figs else None}
+    if dram_frac is not None and (issue["frac"] is None or dram_frac > issue["frac"]):
+        line.update({"bound": "hbm", "achieved": alg, "peak": peak_hbm, "unit": "GB/s", "frac": alg / peak_hbm})
+    else:
+        line.update({"bound": "issue", "achieved": issue["achieved"], "peak": issue_peak,
+                     "unit": "G warp-instructions/s", "frac": issue["frac"]})
     return line
 
 
@@ -443,7 +456,7 @@ def run_mcgb(args, rank, world):
     # Plain FP64 form on the same ladder (one lattice per launch), bounded.
     plain = plain_fp64_rate(batch, sigma, seed) if rank == 0 and not args.skip_plain else None
     # The reference-facing entry points on the same ladder, bounded.
-    dropin = dropin_rate(20 * SWEEPS_PER_STEP, seed)[0] if rank == 0 else None
+    dropin = dropin_rate(20 * SWEEPS_PER_STEP, seed)[0] if rank == 0 and not args.skip_dropin else None
     # A resident launch runs a whole step (10 windows with their exchanges);
     # otherwise one fused launch per window.
     launches = args.steps * batch.launches_per_step(SWEEPS_PER_STEP // EXCHANGE_INTERVAL)
@@ -740,7 +753,7 @@ def run_workload(args, rank, world):
     prof = PROFILE.get(args.workload)
     roofline = roofline_line(profile_figures(prof), prof, n_sites * win, window_ms, BYTES[kind], sm_mhz,
                              f"window_kernel ({kind})" + (f", {len(ws)} launches (size groups)" if len(ws) > 1
-                                                          else ""))
+                                                          else ""), scale_traffic=True)
 
     # End to end: the chain state up from pinned memory, 100 sweeps, the
     # chain state and the step's samples back.
@@ -868,6 +881,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["mcgb", "reference"], default="mcgb")
     ap.add_argument("--skip-plain", action="store_true", help="do not time the plain FP64 form")
+    ap.add_argument("--skip-dropin", action="store_true", help="do not time the drop-in entry points")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: set up the ladder, then launch 6 window kernels and exit")
