@@ -233,13 +233,14 @@ __global__ void he3_reduce_kernel(const float *__restrict__ state, int R, int L,
                                   float g_d, const int32_t *__restrict__ tidx,
                                   const double *__restrict__ cached, double *__restrict__ out)
 {
-    __shared__ double scratch[NC * 32];
-    const int r = blockIdx.x;
+    __shared__ double scratch[NC * 32], part[NC];
+    const ReplicaSpan sp = replica_span();
+    const int r = sp.r;
     double v[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) v[c] = 0.0;
     const bool need_e = cached == nullptr;
-    for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
+    for (int k = sp.first; k < L * L; k += sp.step) {
         const int i = k / L, j = k - i * L;
         const int ip = wrapi(i + 1, L), jp = wrapi(j + 1, L);
         c32 psi[6];
@@ -280,8 +281,8 @@ __global__ void he3_reduce_kernel(const float *__restrict__ state, int R, int L,
             }
         }
     }
-    block_sum<NC>(v, scratch);
-    if (threadIdx.x == 0) {
+    cluster_sum<NC>(v, scratch, part);
+    if (sp.rank == 0 && threadIdx.x == 0) {
         const int dst = tidx ? tidx[r] : r;
         out[dst] = need_e ? v[0] : cached[r];
         if (NC == 10) {
@@ -364,9 +365,9 @@ extern "C" int mcgb_he3_energy(const float *state, int R, int L, const float *co
 {
     if (int st = check_he3("he3_energy", R, L, coefficients)) return st;
     MCGB_REQUIRE(state && out, "he3_energy: null pointer");
-    he3_reduce_kernel<1><<<R, 256, 0, as_stream(stream)>>>(state, R, L, make_coeff(coefficients), K, g_d,
-                                                           nullptr, nullptr, out);
-    return check_launch("he3_reduce_kernel");
+    return launch_replica_reduce(he3_reduce_kernel<1>, R, L, 256, as_stream(stream), "he3_reduce_kernel", state, R,
+                                 L, make_coeff(coefficients), K, g_d, (const int32_t *)nullptr,
+                                 (const double *)nullptr, out);
 }
 
 extern "C" int mcgb_he3_measure(const float *state, int R, int L, const float *coefficients, float K, float g_d,
@@ -374,9 +375,8 @@ extern "C" int mcgb_he3_measure(const float *state, int R, int L, const float *c
 {
     if (int st = check_he3("he3_measure", R, L, coefficients)) return st;
     MCGB_REQUIRE(state && out, "he3_measure: null pointer");
-    he3_reduce_kernel<10><<<R, 256, 0, as_stream(stream)>>>(state, R, L, make_coeff(coefficients), K, g_d,
-                                                            tidx, cached, out);
-    return check_launch("he3_reduce_kernel");
+    return launch_replica_reduce(he3_reduce_kernel<10>, R, L, 256, as_stream(stream), "he3_reduce_kernel", state, R,
+                                 L, make_coeff(coefficients), K, g_d, tidx, cached, out);
 }
 
 extern "C" int mcgb_he3_local_differences(const float *state, int R, int L, const int32_t *positions,

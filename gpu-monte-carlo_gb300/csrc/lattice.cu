@@ -9,7 +9,8 @@
 // r*L*L + i*L + j, every draw is taken whether or not the move is accepted,
 // and each acceptance test is `dE <= 0 or u < expf(-beta*dE)` in float32, as
 // in the reference kernels.  Reductions accumulate in float64 with one
-// thread block per replica (warp shuffles, then one pass over warp sums).
+// thread-block cluster per replica (warp shuffles, a pass over warp sums,
+// then the CTAs' sums in rank order through distributed shared memory).
 #include "mcgb_common.cuh"
 
 namespace mcgb {
@@ -84,22 +85,23 @@ __global__ void ising_reduce_kernel(const int8_t *__restrict__ spins, int R, int
                                     const int32_t *__restrict__ tidx, const double *__restrict__ cached,
                                     double *__restrict__ out, int energy_only)
 {
-    __shared__ double scratch[2 * 32];
-    const int r = blockIdx.x;
+    __shared__ double scratch[2 * 32], part[2];
+    const ReplicaSpan sp = replica_span();
+    const int r = sp.r;
     const int8_t *b = spins + (int64_t)r * L * L;
     // Integer partial sums are exact; J is applied once at the end, which
     // equals the reference's per-bond float64 products for |sum| < 2^53.
     long long e = 0, m = 0;
     const bool need_e = cached == nullptr;
-    for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
+    for (int k = sp.first; k < L * L; k += sp.step) {
         int i = k / L, j = k - i * L;
         int s = b[k];
         if (need_e) e += s * (b[wrapi(i + 1, L) * L + j] + b[i * L + wrapi(j + 1, L)]);
         m += s;
     }
     double v[2] = {(double)e, (double)m};
-    block_sum<2>(v, scratch);
-    if (threadIdx.x == 0) {
+    cluster_sum<2>(v, scratch, part);
+    if (sp.rank == 0 && threadIdx.x == 0) {
         double energy = need_e ? -(double)J * v[0] : cached[r];
         if (energy_only) {
             out[r] = energy;
@@ -206,14 +208,15 @@ __global__ void xy_reduce_kernel(const float *__restrict__ theta, int R, int L, 
                                  const int32_t *__restrict__ tidx, const double *__restrict__ cached,
                                  double *__restrict__ out)
 {
-    __shared__ double scratch[NC * 32];
-    const int r = blockIdx.x;
+    __shared__ double scratch[NC * 32], part[NC];
+    const ReplicaSpan sp = replica_span();
+    const int r = sp.r;
     const float *b = theta + (int64_t)r * L * L;
     double v[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) v[c] = 0.0;
     const bool need_e = cached == nullptr;
-    for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
+    for (int k = sp.first; k < L * L; k += sp.step) {
         const int i = k / L, j = k - i * L;
         const double t = b[k];
         const double dx = t - (double)b[wrapi(i + 1, L) * L + j];
@@ -228,8 +231,8 @@ __global__ void xy_reduce_kernel(const float *__restrict__ theta, int R, int L, 
             v[NC == 5 ? 4 : 0] += sin(dx);
         }
     }
-    block_sum<NC>(v, scratch);
-    if (threadIdx.x == 0) {
+    cluster_sum<NC>(v, scratch, part);
+    if (sp.rank == 0 && threadIdx.x == 0) {
         const int d = tidx ? tidx[r] : r;
         out[d] = need_e ? v[0] : cached[r];
 #pragma unroll
@@ -380,14 +383,15 @@ __global__ void kawamura_reduce_kernel(const float *__restrict__ state, int R, i
                                        const int32_t *__restrict__ tidx,
                                        const double *__restrict__ cached, double *__restrict__ out)
 {
-    __shared__ double scratch[NC * 32];
-    const int r = blockIdx.x;
+    __shared__ double scratch[NC * 32], part[NC];
+    const ReplicaSpan sp = replica_span();
+    const int r = sp.r;
     const float *b = state + (int64_t)r * L * L * 5;
     double v[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) v[c] = 0.0;
     const bool need_e = cached == nullptr;
-    for (int k = threadIdx.x; k < L * L; k += blockDim.x) {
+    for (int k = sp.first; k < L * L; k += sp.step) {
         const int i = k / L, j = k - i * L;
         const float *a = b + (int64_t)k * 5;
         double w, ang;
@@ -413,8 +417,8 @@ __global__ void kawamura_reduce_kernel(const float *__restrict__ state, int R, i
             v[NC == 12 ? 11 : 0] += w * sin(ang);
         }
     }
-    block_sum<NC>(v, scratch);
-    if (threadIdx.x == 0) {
+    cluster_sum<NC>(v, scratch, part);
+    if (sp.rank == 0 && threadIdx.x == 0) {
         const int d = tidx ? tidx[r] : r;
         out[d] = need_e ? v[0] : cached[r];
         if (NC == 12) {
@@ -470,8 +474,8 @@ extern "C" int mcgb_ising_energy(const int8_t *spins, int R, int L, float J, dou
 {
     if (int st = check_lattice("ising_energy", R, L)) return st;
     MCGB_REQUIRE(spins && out, "ising_energy: null pointer");
-    ising_reduce_kernel<<<R, kReduceThreads, 0, as_stream(stream)>>>(spins, R, L, J, nullptr, nullptr, out, 1);
-    return check_launch("ising_reduce_kernel");
+    return launch_replica_reduce(ising_reduce_kernel, R, L, kReduceThreads, as_stream(stream), "ising_reduce_kernel",
+                                 spins, R, L, J, (const int32_t *)nullptr, (const double *)nullptr, out, 1);
 }
 
 extern "C" int mcgb_ising_measure(const int8_t *spins, int R, int L, float J, const int32_t *tidx,
@@ -479,8 +483,8 @@ extern "C" int mcgb_ising_measure(const int8_t *spins, int R, int L, float J, co
 {
     if (int st = check_lattice("ising_measure", R, L)) return st;
     MCGB_REQUIRE(spins && out, "ising_measure: null pointer");
-    ising_reduce_kernel<<<R, kReduceThreads, 0, as_stream(stream)>>>(spins, R, L, J, tidx, cached, out, 0);
-    return check_launch("ising_reduce_kernel");
+    return launch_replica_reduce(ising_reduce_kernel, R, L, kReduceThreads, as_stream(stream), "ising_reduce_kernel",
+                                 spins, R, L, J, tidx, cached, out, 0);
 }
 
 extern "C" int mcgb_xy_update_color(float *theta, void *rng, const float *betas, int R, int L, int color,
@@ -544,8 +548,8 @@ extern "C" int mcgb_xy_energy(const float *theta, int R, int L, float J, double 
 {
     if (int st = check_lattice("xy_energy", R, L)) return st;
     MCGB_REQUIRE(theta && out, "xy_energy: null pointer");
-    xy_reduce_kernel<1><<<R, kReduceThreads, 0, as_stream(stream)>>>(theta, R, L, J, nullptr, nullptr, out);
-    return check_launch("xy_reduce_kernel");
+    return launch_replica_reduce(xy_reduce_kernel<1>, R, L, kReduceThreads, as_stream(stream), "xy_reduce_kernel",
+                                 theta, R, L, J, (const int32_t *)nullptr, (const double *)nullptr, out);
 }
 
 extern "C" int mcgb_xy_measure(const float *theta, int R, int L, float J, const int32_t *tidx,
@@ -553,8 +557,8 @@ extern "C" int mcgb_xy_measure(const float *theta, int R, int L, float J, const 
 {
     if (int st = check_lattice("xy_measure", R, L)) return st;
     MCGB_REQUIRE(theta && out, "xy_measure: null pointer");
-    xy_reduce_kernel<5><<<R, kReduceThreads, 0, as_stream(stream)>>>(theta, R, L, J, tidx, cached, out);
-    return check_launch("xy_reduce_kernel");
+    return launch_replica_reduce(xy_reduce_kernel<5>, R, L, kReduceThreads, as_stream(stream), "xy_reduce_kernel",
+                                 theta, R, L, J, tidx, cached, out);
 }
 
 extern "C" int mcgb_kawamura_update_color(float *state, void *rng, const float *betas, int R, int L,
@@ -573,8 +577,9 @@ extern "C" int mcgb_kawamura_energy(const float *state, int R, int L, float J, d
 {
     if (int st = check_lattice("kawamura_energy", R, L)) return st;
     MCGB_REQUIRE(state && out, "kawamura_energy: null pointer");
-    kawamura_reduce_kernel<1><<<R, kReduceThreads, 0, as_stream(stream)>>>(state, R, L, J, nullptr, nullptr, out);
-    return check_launch("kawamura_reduce_kernel");
+    return launch_replica_reduce(kawamura_reduce_kernel<1>, R, L, kReduceThreads, as_stream(stream),
+                                 "kawamura_reduce_kernel", state, R, L, J, (const int32_t *)nullptr,
+                                 (const double *)nullptr, out);
 }
 
 extern "C" int mcgb_kawamura_measure(const float *state, int R, int L, float J, const int32_t *tidx,
@@ -582,8 +587,8 @@ extern "C" int mcgb_kawamura_measure(const float *state, int R, int L, float J, 
 {
     if (int st = check_lattice("kawamura_measure", R, L)) return st;
     MCGB_REQUIRE(state && out, "kawamura_measure: null pointer");
-    kawamura_reduce_kernel<12><<<R, kReduceThreads, 0, as_stream(stream)>>>(state, R, L, J, tidx, cached, out);
-    return check_launch("kawamura_reduce_kernel");
+    return launch_replica_reduce(kawamura_reduce_kernel<12>, R, L, kReduceThreads, as_stream(stream),
+                                 "kawamura_reduce_kernel", state, R, L, J, tidx, cached, out);
 }
 
 extern "C" int mcgb_kawamura_local_energies(const float *state, int R, int L, const int32_t *positions,

@@ -8,6 +8,7 @@
 //   algebra uses (models/he3/update.py).
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -113,5 +114,86 @@ __device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch)
 }
 
 __host__ __device__ __forceinline__ int wrapi(int i, int L) { return i < 0 ? i + L : (i >= L ? i - L : i); }
+
+// ---------------------------------------------------------------- per-replica reductions on a cluster
+//
+// A per-replica reduction launched by launch_replica_reduce runs one
+// thread-block cluster of C CTAs per replica (blockIdx.x / C): CTA `rank`
+// takes sites k = rank * blockDim.x + threadIdx.x, k + C * blockDim.x, ...;
+// cluster_sum adds the CTAs' block sums in rank order through distributed
+// shared memory.  The order of every addition is fixed by the launch shape,
+// so results are reproducible, and no global scratch is needed.
+
+struct ReplicaSpan {
+    int r, rank, first, step;
+};
+
+__device__ __forceinline__ ReplicaSpan replica_span()
+{
+    namespace cg = cooperative_groups;
+    const cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks();
+    return ReplicaSpan{(int)(blockIdx.x / C), (int)cl.block_rank(), (int)(cl.block_rank() * blockDim.x + threadIdx.x),
+                       (int)(C * blockDim.x)};
+}
+
+// Sum of NC channels over the CTA (block_sum), then over the cluster's CTAs
+// in rank order: valid in thread 0 of rank 0.  `scratch` holds 32*NC
+// doubles, `part` NC doubles of shared memory.  Every thread must call it.
+template <int NC>
+__device__ __forceinline__ void cluster_sum(double (&v)[NC], double *scratch, double *part)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    block_sum<NC>(v, scratch);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) part[c] = v[c];
+    }
+    cl.sync();
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) v[c] = part[c];
+        for (unsigned k = 1; k < cl.num_blocks(); ++k) {
+            const double *pk = cl.map_shared_rank(part, k);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] += pk[c];
+        }
+    }
+    // Peers keep their shared memory until rank 0 has read it.
+    cl.sync();
+}
+
+// CTAs per replica: enough clusters to give every SM about two CTAs, at
+// most 8 (the portable cluster size) and at most one CTA per `threads`
+// sites.
+int replica_reduce_cluster(int R, int L, int threads);
+
+// Launch `kern` as one cluster of replica_reduce_cluster(R, L, threads) CTAs
+// per replica.
+template <typename... KArgs, typename... Args>
+int launch_replica_reduce(void (*kern)(KArgs...), int R, int L, int threads, cudaStream_t s, const char *name,
+                          Args... args)
+{
+    const int C = replica_reduce_cluster(R, L, threads);
+    if (C < 0) return C;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(R * C));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t err = cudaLaunchKernelEx(&cfg, kern, args...);
+    if (err != cudaSuccess) {
+        (void)cudaGetLastError();  // a refused configuration is not sticky
+        return cuda_status(err, name);
+    }
+    return check_launch(name);
+}
 
 }  // namespace mcgb

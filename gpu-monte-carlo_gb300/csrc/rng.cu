@@ -42,6 +42,22 @@ int check_launch(const char *what)
     return cuda_status(cudaGetLastError(), what);
 }
 
+int replica_reduce_cluster(int R, int L, int threads)
+{
+    int dev = 0, sms = 0;
+    int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st) return st;
+    st = cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                     "cudaDeviceGetAttribute(multiprocessors)");
+    if (st) return st;
+    long long C = (2LL * sms + R - 1) / R;
+    const long long by_sites = (long long)L * L / threads;
+    if (C > by_sites) C = by_sites;
+    if (C > 8) C = 8;
+    if (C < 1) C = 1;
+    return (int)C;
+}
+
 // ------------------------------------------------------------ jump tables
 
 constexpr int kJumpLevels = 48;
