@@ -125,15 +125,17 @@ __device__ __forceinline__ float xy_bond_sum(const float *b, int L, int i, int j
     return ((cosf(t - up) + cosf(t - down)) + cosf(t - left)) + cosf(t - right);
 }
 
+// Colour `color` (ncol = 1) or colours `color` and `color` + 1 (ncol = 2:
+// colours 1 and 2 share no bond, so one launch of both equals two).
 template <bool kGauss>
 __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restrict__ rng,
                                 const float *__restrict__ betas, const float *__restrict__ sigmas,
-                                int R, int L, int color, float J, float delta)
+                                int R, int L, int color, int ncol, float J, float delta)
 {
     const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
     int r, i, j;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!color_site(t, R, L, color, r, i, j)) return;
+    if (!phase_site(t, R, L, color, ncol, r, i, j)) return;
     float *b = theta + (int64_t)r * L * L;
     const float th = b[i * L + j];
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
@@ -300,14 +302,15 @@ __device__ __forceinline__ float kaw_local_energy(const float *b, int L, int i, 
     return energy;
 }
 
+// Colour `color`, or colours `color` and `color` + 1 with ncol = 2 (as xy_color_kernel).
 __global__ void kawamura_color_kernel(float *__restrict__ state, ulonglong2 *__restrict__ rng,
-                                      const float *__restrict__ betas, int R, int L, int color,
+                                      const float *__restrict__ betas, int R, int L, int color, int ncol,
                                       float J, float delta)
 {
     const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
     int r, i, j;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!color_site(t, R, L, color, r, i, j)) return;
+    if (!phase_site(t, R, L, color, ncol, r, i, j)) return;
     const float *b = state + (int64_t)r * L * L * 5;
     float *site = state + (((int64_t)r * L + i) * L + j) * 5;
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
@@ -495,7 +498,7 @@ extern "C" int mcgb_xy_update_color(float *theta, void *rng, const float *betas,
     MCGB_REQUIRE(color >= 0 && color < 4, "xy_update_color: color must be 0..3");
     const int64_t n = (int64_t)R * (L / 2) * (L / 2);
     xy_color_kernel<false><<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
-        theta, static_cast<ulonglong2 *>(rng), betas, nullptr, R, L, color, J, delta);
+        theta, static_cast<ulonglong2 *>(rng), betas, nullptr, R, L, color, 1, J, delta);
     return check_launch("xy_color_kernel");
 }
 
@@ -507,7 +510,30 @@ extern "C" int mcgb_xy_update_color_gauss(float *theta, void *rng, const float *
     MCGB_REQUIRE(color >= 0 && color < 4, "xy_update_color_gauss: color must be 0..3");
     const int64_t n = (int64_t)R * (L / 2) * (L / 2);
     xy_color_kernel<true><<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
-        theta, static_cast<ulonglong2 *>(rng), betas, sigmas, R, L, color, J, 0.0f);
+        theta, static_cast<ulonglong2 *>(rng), betas, sigmas, R, L, color, 1, J, 0.0f);
+    return check_launch("xy_color_kernel");
+}
+
+extern "C" int mcgb_xy_sweep(float *theta, void *rng, const float *betas, const float *sigmas, int R, int L,
+                             float J, float delta, int n_sweeps, void *stream)
+{
+    if (int st = check_lattice("xy_sweep", R, L)) return st;
+    MCGB_REQUIRE(theta && rng && betas, "xy_sweep: null pointer");
+    MCGB_REQUIRE(n_sweeps >= 0, "xy_sweep: n_sweeps must be >= 0");
+    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
+    cudaStream_t s = as_stream(stream);
+    ulonglong2 *st = static_cast<ulonglong2 *>(rng);
+    for (int k = 0; k < n_sweeps; ++k) {
+        for (int ph = 0; ph < 3; ++ph) {
+            const int c0 = ph == 0 ? 0 : (ph == 1 ? 1 : 3), ncol = ph == 1 ? 2 : 1;
+            if (sigmas)
+                xy_color_kernel<true><<<grid_for(ncol * n, kColorThreads), kColorThreads, 0, s>>>(
+                    theta, st, betas, sigmas, R, L, c0, ncol, J, 0.0f);
+            else
+                xy_color_kernel<false><<<grid_for(ncol * n, kColorThreads), kColorThreads, 0, s>>>(
+                    theta, st, betas, nullptr, R, L, c0, ncol, J, delta);
+        }
+    }
     return check_launch("xy_color_kernel");
 }
 
@@ -569,7 +595,25 @@ extern "C" int mcgb_kawamura_update_color(float *state, void *rng, const float *
     MCGB_REQUIRE(color >= 0 && color < 4, "kawamura_update_color: color must be 0..3");
     const int64_t n = (int64_t)R * (L / 2) * (L / 2);
     kawamura_color_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
-        state, static_cast<ulonglong2 *>(rng), betas, R, L, color, J, delta);
+        state, static_cast<ulonglong2 *>(rng), betas, R, L, color, 1, J, delta);
+    return check_launch("kawamura_color_kernel");
+}
+
+extern "C" int mcgb_kawamura_sweep(float *state, void *rng, const float *betas, int R, int L, float J,
+                                   float delta, int n_sweeps, void *stream)
+{
+    if (int st = check_lattice("kawamura_sweep", R, L)) return st;
+    MCGB_REQUIRE(state && rng && betas, "kawamura_sweep: null pointer");
+    MCGB_REQUIRE(n_sweeps >= 0, "kawamura_sweep: n_sweeps must be >= 0");
+    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
+    cudaStream_t s = as_stream(stream);
+    for (int k = 0; k < n_sweeps; ++k) {
+        for (int ph = 0; ph < 3; ++ph) {
+            const int c0 = ph == 0 ? 0 : (ph == 1 ? 1 : 3), ncol = ph == 1 ? 2 : 1;
+            kawamura_color_kernel<<<grid_for(ncol * n, kColorThreads), kColorThreads, 0, s>>>(
+                state, static_cast<ulonglong2 *>(rng), betas, R, L, c0, ncol, J, delta);
+        }
+    }
     return check_launch("kawamura_color_kernel");
 }
 

@@ -31,12 +31,14 @@ SIGNATURES = {
     "mcgb_ising_measure": [_P, _I, _I, _F, _P, _P, _P, _P],
     "mcgb_xy_update_color": [_P, _P, _P, _I, _I, _I, _F, _F, _P],
     "mcgb_xy_update_color_gauss": [_P, _P, _P, _P, _I, _I, _I, _F, _P],
+    "mcgb_xy_sweep": [_P, _P, _P, _P, _I, _I, _F, _F, _I, _P],
     "mcgb_xy64_update_color": [_P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _P],
     "mcgb_xy64_energy": [_P, _I, _I, _I, _D, _P, _P],
     "mcgb_xy64_measure": [_P, _I, _I, _I, _D, _P, _P, _P],
     "mcgb_xy_energy": [_P, _I, _I, _F, _P, _P],
     "mcgb_xy_measure": [_P, _I, _I, _F, _P, _P, _P, _P],
     "mcgb_kawamura_update_color": [_P, _P, _P, _I, _I, _I, _F, _F, _P],
+    "mcgb_kawamura_sweep": [_P, _P, _P, _I, _I, _F, _F, _I, _P],
     "mcgb_kawamura_energy": [_P, _I, _I, _F, _P, _P],
     "mcgb_kawamura_measure": [_P, _I, _I, _F, _P, _P, _P, _P],
     "mcgb_kawamura_local_energies": [_P, _I, _I, _P, _P, _I, _F, _P, _P],

@@ -39,6 +39,20 @@ class KawamuraModel(Model):
         _lib.call("mcgb_kawamura_update_color", ptr(state), ptr(rng_states), ptr(betas), R, L,
                   int(color), float(self.J), float(self.delta), _lib.stream_handle())
 
+    def enqueue_sweep(self, state, rng_states, betas):
+        """One whole sweep in three launches (colours 0, {1, 2}, 3: colours 1
+        and 2 share no bond), bit-identical to four update_color calls.
+        Returns False, enqueueing nothing, when a subclass or the instance
+        replaced update_color, so that its own colour updates run instead."""
+        if type(self).update_color is not KawamuraModel.update_color or "update_color" in vars(self):
+            return False
+        R, L = geometry(state, np.float32, (5,), "KawamuraModel.enqueue_sweep")
+        check_rng(rng_states, R, L, "KawamuraModel.enqueue_sweep")
+        check_vector(betas, R, np.float32, "KawamuraModel.enqueue_sweep", "betas")
+        _lib.call("mcgb_kawamura_sweep", ptr(state), ptr(rng_states), ptr(betas), R, L, float(self.J),
+                  float(self.delta), 1, _lib.stream_handle())
+        return True
+
     measurement_names = MEASUREMENT_NAMES
 
     def measure_into(self, state, out, temperature_indices=None, cached_energies=None):

@@ -52,6 +52,26 @@ class XYModel(Model):
             _lib.call("mcgb_xy_update_color_gauss", ptr(state), ptr(rng_states), ptr(betas),
                       ptr(self.sigmas), R, L, int(color), float(self.J), _lib.stream_handle())
 
+    def enqueue_sweep(self, state, rng_states, betas):
+        """One whole sweep in three launches (colours 0, {1, 2}, 3: colours 1
+        and 2 share no bond), bit-identical to four update_color calls.
+        Returns False, enqueueing nothing, when a subclass or the instance
+        replaced update_color, so that its own colour updates run instead."""
+        if type(self).update_color is not XYModel.update_color or "update_color" in vars(self):
+            return False
+        R, L = geometry(state, np.float32, (), "XYModel.enqueue_sweep")
+        check_rng(rng_states, R, L, "XYModel.enqueue_sweep")
+        check_vector(betas, R, np.float32, "XYModel.enqueue_sweep", "betas")
+        sig = None
+        if self.proposal == "gaussian":
+            if self.sigmas is None:
+                raise ValueError("Gaussian proposals need per-walker sigmas")
+            check_vector(self.sigmas, R, np.float32, "XYModel.enqueue_sweep", "sigmas")
+            sig = ptr(self.sigmas)
+        _lib.call("mcgb_xy_sweep", ptr(state), ptr(rng_states), ptr(betas), sig, R, L, float(self.J),
+                  float(self.delta), 1, _lib.stream_handle())
+        return True
+
     measurement_names = MEASUREMENT_NAMES
 
     def measure_into(self, state, out, temperature_indices=None, cached_energies=None):

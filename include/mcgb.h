@@ -85,6 +85,13 @@ int mcgb_xy_update_color(float *theta, void *rng, const float *betas, int R, int
 int mcgb_xy_update_color_gauss(float *theta, void *rng, const float *betas,
                                const float *sigmas, int R, int L, int color, float J,
                                void *stream);
+/* A whole sweep (core/runtime.py:87-99: colours 0, 1, 2, 3 of
+ * models/xy/update.py:6-54, or of the Gaussian proposal when sigmas is not
+ * NULL) in three launches per sweep -- colours 0, {1, 2}, 3: colours 1 and
+ * 2 share no bond -- bit-identical to four update_color calls; n_sweeps
+ * sweeps. */
+int mcgb_xy_sweep(float *theta, void *rng, const float *betas, const float *sigmas, int R, int L,
+                  float J, float delta, int n_sweeps, void *stream);
 /* Plain FP64 form: one lattice (replica r) per launch, float64 state,
  * float64 betas and sigmas, float64 uniforms; sigmas NULL = uniform delta.
  * With w2t NULL, betas and sigmas are per walker; otherwise they are per
@@ -114,6 +121,11 @@ int mcgb_xy_measure(const float *theta, int R, int L, float J,
  * models/kawamura/update.py:21-65 (three sub-moves, six draws per visit). */
 int mcgb_kawamura_update_color(float *state, void *rng, const float *betas, int R, int L,
                                int color, float J, float delta, void *stream);
+/* A whole sweep (core/runtime.py:87-99 over models/kawamura/update.py:7-65)
+ * in three launches, colours 0, {1, 2}, 3, bit-identical to four
+ * update_color calls; n_sweeps sweeps. */
+int mcgb_kawamura_sweep(float *state, void *rng, const float *betas, int R, int L, float J, float delta,
+                        int n_sweeps, void *stream);
 /* models/kawamura/measure.py:96-122. */
 int mcgb_kawamura_energy(const float *state, int R, int L, float J, double *out, void *stream);
 /* models/kawamura/measure.py:14-93: out (7, R) = energy, chirality, px, py,

@@ -396,3 +396,42 @@ def test_he3_hot_moves_and_cold_minimum():
     for _ in range(4):
         cold.sweep()
     np.testing.assert_allclose(cold.measure()["energy"], e0, atol=1e-5)
+
+
+@pytest.mark.parametrize("kind", ["ising", "xy", "xy_gauss", "kawamura"])
+def test_fused_sweep_equals_four_colour_launches(kind):
+    """Runtime.sweep of an unmodified built-in model runs colours 0, {1, 2}, 3
+    in three launches (colours 1 and 2 share no bond): bit-identical to the
+    reference's four update_color calls, streams included."""
+    from mcgb.core.runtime import Runtime
+    from mcgb.device import to_device
+    from mcgb.models.ising.model import IsingModel
+    from mcgb.models.kawamura.model import KawamuraModel
+    from mcgb.models.xy.model import XYModel
+    R, L, seed = 3, 16, 31
+    r = np.random.default_rng(7)
+    if kind == "ising":
+        make, init = (lambda: IsingModel()), r.choice(np.array([-1, 1], np.int8), (R, L, L))
+    elif kind.startswith("xy"):
+        sig = to_device(np.array([0.9, 1.2, 1.5], np.float32))
+        make = (lambda: XYModel(proposal="gaussian", sigmas=sig)) if kind == "xy_gauss" else (lambda: XYModel())
+        init = r.uniform(-np.pi, np.pi, (R, L, L)).astype(np.float32)
+    else:
+        make = lambda: KawamuraModel()  # noqa: E731
+        init = np.zeros((R, L, L, 5), np.float32)
+        init[..., 0] = r.uniform(-np.pi, np.pi, (R, L, L))
+        init[..., 1] = r.choice([-1.0, 1.0], (R, L, L))
+        d = r.normal(size=(R, L, L, 3))
+        init[..., 2:] = d / np.linalg.norm(d, axis=-1, keepdims=True)
+    T = [0.8, 1.5, 2.5]
+    a, b = Runtime(make(), L, T, seed=seed), Runtime(make(), L, T, seed=seed)
+    for rt in (a, b):
+        rt.state.copy_to_device(init)
+    for _ in range(3):
+        a.sweep()
+        for c in range(4):
+            b.model.update_color(b.state, b.rng_states, b.betas, c, b.blocks_per_grid, b.threads_per_block)
+    np.testing.assert_array_equal(a.snapshot(), b.snapshot())
+    ra, rb = a.rng_states.copy_to_host(), b.rng_states.copy_to_host()
+    np.testing.assert_array_equal(ra["s0"], rb["s0"])
+    np.testing.assert_array_equal(ra["s1"], rb["s1"])
