@@ -222,7 +222,13 @@ __global__ void xy_reduce_kernel(const float *__restrict__ theta, int R, int L, 
         const int i = k / L, j = k - i * L;
         const double t = b[k];
         const double dx = t - (double)b[wrapi(i + 1, L) * L + j];
-        const double cos_x = cos(dx);
+        // cos and sin of the x-bond angle from one argument reduction when
+        // both are needed (the float64 pipe is the bound of this kernel).
+        double cos_x, sin_x = 0.0;
+        if (NC == 5)
+            sincos(dx, &sin_x, &cos_x);
+        else
+            cos_x = cos(dx);
         if (need_e) v[0] += -(double)J * (cos_x + cos(t - (double)b[i * L + wrapi(j + 1, L)]));
         if (NC == 5) {
             double sn, cs;
@@ -230,7 +236,7 @@ __global__ void xy_reduce_kernel(const float *__restrict__ theta, int R, int L, 
             v[NC == 5 ? 1 : 0] += cs;
             v[NC == 5 ? 2 : 0] += sn;
             v[NC == 5 ? 3 : 0] += cos_x;
-            v[NC == 5 ? 4 : 0] += sin(dx);
+            v[NC == 5 ? 4 : 0] += sin_x;
         }
     }
     cluster_sum<NC>(v, scratch, part);
@@ -379,6 +385,16 @@ __device__ __forceinline__ double kaw_bond64(const float *a, const float *n, dou
     return weight * cos(angle);
 }
 
+// The same bond with sin(angle) too, from one argument reduction.
+__device__ __forceinline__ double kaw_bond64_sc(const float *a, const float *n, double &weight, double &sin_angle)
+{
+    const double dot = (double)a[2] * n[2] + (double)a[3] * n[3] + (double)a[4] * n[4];
+    weight = (1.0 + (double)a[1] * n[1]) * dot;
+    double c;
+    sincos((double)a[0] - (double)n[0], &sin_angle, &c);
+    return weight * c;
+}
+
 // models/kawamura/measure.py:14-122.  NC = 1 energy only; NC = 12 sums for
 // the 7 output channels (spin2 is formed from 6 tensor sums at the end).
 template <int NC>
@@ -397,8 +413,9 @@ __global__ void kawamura_reduce_kernel(const float *__restrict__ state, int R, i
     for (int k = sp.first; k < L * L; k += sp.step) {
         const int i = k / L, j = k - i * L;
         const float *a = b + (int64_t)k * 5;
-        double w, ang;
-        const double cx = kaw_bond64(a, b + ((int64_t)wrapi(i + 1, L) * L + j) * 5, w, ang);
+        double w, ang, sin_x = 0.0;
+        const float *nx = b + ((int64_t)wrapi(i + 1, L) * L + j) * 5;
+        const double cx = NC == 12 ? kaw_bond64_sc(a, nx, w, sin_x) : kaw_bond64(a, nx, w, ang);
         if (need_e) {
             double w2, ang2;
             v[0] -= (double)J * (cx + kaw_bond64(a, b + ((int64_t)i * L + wrapi(j + 1, L)) * 5, w2, ang2));
@@ -417,7 +434,7 @@ __global__ void kawamura_reduce_kernel(const float *__restrict__ state, int R, i
             v[NC == 12 ? 8 : 0] += dx * dz;
             v[NC == 12 ? 9 : 0] += dy * dz;
             v[NC == 12 ? 10 : 0] += cx;
-            v[NC == 12 ? 11 : 0] += w * sin(ang);
+            v[NC == 12 ? 11 : 0] += w * sin_x;
         }
     }
     cluster_sum<NC>(v, scratch, part);
