@@ -10,7 +10,9 @@
 // barrier, colour 3, barrier -- the visit order of four sequential colour
 // launches, since every site draws from its own stream.  Models whose sites
 // couple colours 1 and 2 (He3's diagonal gradient cells) set kSplitMiddle and
-// get a barrier between them.  A sample due after a sweep is measured by
+// get a barrier between them.  The others, whose colours 0 and 3 share no
+// bond either, run colour 0 of the next sweep in the colour-3 phase within a
+// window (two barriers a sweep instead of three).  A sample due after a sweep is measured by
 // every CTA, reduced over the CTA in compensated float32 and pushed into
 // rank 0's shared memory before the barrier that ends the sweep; one warp of
 // rank 0 combines the partial sums after the next wait and writes the sample
@@ -882,10 +884,26 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         pend = -1;                                                                                          \
     }
         [[maybe_unused]] typename M::Prop pa[NK], pb[NK];
+        // Colour 0 of this sweep already ran, in the last phase of the
+        // previous sweep (see `merge` below).
+        bool c0_done = false;
         for (int s = 0; s < cm.n_sweeps; ++s) {
             // This sweep's accepted energy changes (at most a few terms per
             // thread), folded into the compensated running sum once per sweep.
             float dacc = 0.0f;
+            // Colours 0 and 3 share no bond when a site couples to its four
+            // nearest neighbours only (every model without diagonal cells,
+            // i.e. without kSplitMiddle): both read only planes 1 and 2.  So
+            // colour 0 of the next sweep runs in this sweep's colour-3 phase
+            // -- the same moves with the same streams against the same
+            // neighbour values as in a phase of its own -- which saves one
+            // cluster barrier a sweep.  Not after the window's last sweep
+            // (an exchange may change the temperature before the next one)
+            // nor after a sampled sweep (the sample reads the state between
+            // the two).
+            const bool sample_due = sweep0 + s + 1 == next_sample;
+            [[maybe_unused]] const bool merge =
+                !M::kSplitMiddle && (M::kPipeline || !regs) && s + 1 < cm.n_sweeps && !sample_due;
             if constexpr (!M::kPipeline && regs) {
                 {
                     cluster_wait();
@@ -907,14 +925,17 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 {
                 // Invariant: this thread has arrived at the barrier that
                 // follows the previous phase and not yet waited.
-                propose_pass<M, NK, 0, SS>(ctx, cells, own, g, sites, st, pa, sst);
-                cluster_wait();
-                MCGB_COMBINE_PENDING()
-                decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dacc, nacc);
-                cluster_arrive();
+                if (!c0_done) {
+                    propose_pass<M, NK, 0, SS>(ctx, cells, own, g, sites, st, pa, sst);
+                    cluster_wait();
+                    MCGB_COMBINE_PENDING()
+                    decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pa, dacc, nacc);
+                    cluster_arrive();
+                }
                 propose_pass<M, NK, 1, SS>(ctx, cells, own, g, sites, st, pa, sst);
                 propose_pass<M, NK, 2, SS>(ctx, cells, own, g, sites, st, pb, sst);
                 cluster_wait();
+                MCGB_COMBINE_PENDING()
                 decide_pass<M, NK, 1>(ctx, cells, own, g, sites, pa, dacc, nacc);
                 if (M::kSplitMiddle) {
                     cluster_arrive();
@@ -923,16 +944,21 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 decide_pass<M, NK, 2>(ctx, cells, own, g, sites, pb, dacc, nacc);
                 cluster_arrive();
                 propose_pass<M, NK, 3, SS>(ctx, cells, own, g, sites, st, pa, sst);
+                if (merge) propose_pass<M, NK, 0, SS>(ctx, cells, own, g, sites, st, pb, sst);
                 cluster_wait();
                 decide_pass<M, NK, 3>(ctx, cells, own, g, sites, pa, dacc, nacc);
+                if (merge) decide_pass<M, NK, 0>(ctx, cells, own, g, sites, pb, dacc, nacc);
                 }
             } else {
                 (void)sites;
+                if (!c0_done) {
+                    cluster_wait();
+                    MCGB_COMBINE_PENDING()
+                    global_rng_pass<M, 0, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
+                    cluster_arrive();
+                }
                 cluster_wait();
                 MCGB_COMBINE_PENDING()
-                global_rng_pass<M, 0, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
-                cluster_arrive();
-                cluster_wait();
                 global_rng_pass<M, 1, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
                 if (M::kSplitMiddle) {
                     cluster_arrive();
@@ -942,7 +968,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 cluster_arrive();
                 cluster_wait();
                 global_rng_pass<M, 3, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
+                if (merge) global_rng_pass<M, 0, GIF>(a, ctx, cells, own, g, base, gplane, dacc, nacc);
             }
+            c0_done = merge;
 
             comp_add(dsum, dcomp, dacc);
             if (sweep0 + s + 1 == next_sample) {
