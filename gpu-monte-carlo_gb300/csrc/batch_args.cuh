@@ -214,7 +214,8 @@ inline bool smem_streams_fit(size_t smem, int threads)
 // the larger register budget) whenever the thread count allows it; else the
 // global-memory streams, two visits in flight when the policy allows it and
 // the CTA has at most kPairThreads threads (kGlobalPairVariant), one
-// otherwise (NPMAX = 0).
+// otherwise (NPMAX = 0).  A policy with kPairThreads = 0 has no
+// two-plaquette variant.
 template <class M>
 int pick_npmax(const mcgb_batch_window &w)
 {
@@ -239,7 +240,9 @@ int launch_any(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s, c
     MCGB_REQUIRE(w.threads <= M::kMaxThreads, "%s: at most %d threads per CTA", name, M::kMaxThreads);
     switch (pick_npmax<M>(w)) {
     case 1: return launch_window<M, 1>(a, w, s, name);
-    case 2: return launch_window<M, 2>(a, w, s, name);
+    case 2:
+        if constexpr (M::kPairThreads > 0) return launch_window<M, 2>(a, w, s, name);
+        return launch_window<M, 0>(a, w, s, name);
     case kGlobalPairVariant:
         if constexpr (M::kGlobalInFlight == 2) return launch_window<M, kGlobalPairVariant>(a, w, s, name);
         return launch_window<M, 0>(a, w, s, name);
@@ -288,9 +291,11 @@ int max_clusters_any(int C, int threads, size_t smem, int *out)
         if (int st = max_clusters_for<M, 1>(C, threads, smem, &n)) return st;
         if (n < best) best = n;
     }
-    if (threads <= window_max_threads<M, 2>()) {
-        if (int st = max_clusters_for<M, 2>(C, threads, smem, &n)) return st;
-        if (n < best) best = n;
+    if constexpr (M::kPairThreads > 0) {
+        if (threads <= window_max_threads<M, 2>()) {
+            if (int st = max_clusters_for<M, 2>(C, threads, smem, &n)) return st;
+            if (n < best) best = n;
+        }
     }
     if constexpr (M::kGlobalInFlight == 2) {
         if (threads <= window_max_threads<M, kGlobalPairVariant>()) {

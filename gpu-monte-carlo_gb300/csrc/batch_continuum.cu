@@ -280,32 +280,46 @@ struct He3Nbrs {
     const He3Cell *R, *U, *Lf, *D, *LU, *DR;  // (i+1,j) (i,j+1) (i-1,j) (i,j-1) (i-1,j+1) (i+1,j-1)
 };
 
-// Exact change of the three gradient cells containing the site when its
-// components change from cur to nxt (models/he3/update.py:95-175).
-__device__ __forceinline__ float he3_grad_diff(const He3Nbrs &n, const He3Cell &cur, const c32 *nxt)
+// Component mu of the exact change of the three gradient cells containing
+// the site when it moves by (ex, ey) from (x, y) (models/he3/update.py:95-175):
+//   2 Re(conj(ex) fx + conj(ey) fy) + 8 (|ex|^2 + |ey|^2) + 4 Re(conj(ex) ey)
+// with fx, fy from neighbour differences (small in an ordered state, so
+// little is lost to cancellation).  fx - 8x - 2y and fy - 2x - 8y are the
+// neighbour field of the conditional Gaussian proposal
+// (gaussian_fast.py:26-39): one set of neighbour reads serves both.
+struct He3Grad {
+    c32 fx, fy;
+};
+
+__device__ __forceinline__ He3Grad he3_grad_terms(const He3Nbrs &n, int kx, int ky, c32 x, c32 y)
 {
-    float dg = 0.0f;
-#pragma unroll
-    for (int mu = 0; mu < 3; ++mu) {
-        const int kx = 2 * mu, ky = 2 * mu + 1;
-        const c32 x = cur.z[kx], y = cur.z[ky];
-        const c32 ex = nxt[kx] - x, ey = nxt[ky] - y;
-        const c32 a = n.R->z[kx] - x, b = n.R->z[ky] - y, c = n.U->z[kx] - x, d = n.U->z[ky] - y;
-        const c32 al = x - n.Lf->z[kx], bl = y - n.Lf->z[ky], cl = n.LU->z[kx] - n.Lf->z[kx],
-                  dl = n.LU->z[ky] - n.Lf->z[ky];
-        const c32 ad = n.DR->z[kx] - n.D->z[kx], bd = n.DR->z[ky] - n.D->z[ky], cd = x - n.D->z[kx],
-                  dd = y - n.D->z[ky];
-        const c32 fx = (-(3.0f * a + b + c + d) + (3.0f * al + dl)) + (cd + bd);
-        const c32 fy = (-(a + b + c + 3.0f * d) + (bl + cl)) + (3.0f * dd + ad);
-        const float linear = 2.0f * (conj(ex) * fx + conj(ey) * fy).re;
-        const float quadratic = 8.0f * (norm2(ex) + norm2(ey)) + 4.0f * (conj(ex) * ey).re;
-        dg += linear + quadratic;
-    }
-    return dg;
+    const c32 a = n.R->z[kx] - x, b = n.R->z[ky] - y, c = n.U->z[kx] - x, d = n.U->z[ky] - y;
+    const c32 al = x - n.Lf->z[kx], bl = y - n.Lf->z[ky], cl = n.LU->z[kx] - n.Lf->z[kx],
+              dl = n.LU->z[ky] - n.Lf->z[ky];
+    const c32 ad = n.DR->z[kx] - n.D->z[kx], bd = n.DR->z[ky] - n.D->z[ky], cd = x - n.D->z[kx],
+              dd = y - n.D->z[ky];
+    He3Grad g;
+    g.fx = (-(3.0f * a + b + c + d) + (3.0f * al + dl)) + (cd + bd);
+    g.fy = (-(a + b + c + 3.0f * d) + (bl + cl)) + (3.0f * dd + ad);
+    return g;
 }
 
+__device__ __forceinline__ float he3_grad_change(const He3Grad &g, c32 ex, c32 ey)
+{
+    const float linear = 2.0f * (conj(ex) * g.fx + conj(ey) * g.fy).re;
+    const float quadratic = 8.0f * (norm2(ex) + norm2(ey)) + 4.0f * (conj(ex) * ey).re;
+    return linear + quadratic;
+}
+
+// Per-replica constants of a window.  The conditional Gaussian's proposal
+// widths and density coefficients depend on beta, K, rho and the proposal
+// mass only (gaussian_fast.py:57-66), so they are evaluated once per window
+// rather than per visit: sp, sm the widths of the (x+y) and (x-y) noise, qp,
+// qm the coefficients of the reverse/forward log density ratio, kp = -K/plus,
+// km = -K/minus the factors of the neighbour mean.
 struct He3Ctx {
-    float beta, K, delta, g_d, rho, mass;
+    float beta, K, delta, g_d, rho;
+    float sp, sm, qp, qm, kp, km;
     float coeff[5];
     long long *nonfinite;  // counters row 2 entry of this replica
 };
@@ -333,7 +347,12 @@ __device__ __forceinline__ c32 he3_normal_pair(ulonglong2 &st)
 // decision.  Out of line and independent of the colour (the neighbours come
 // as pointers), so the window kernel holds one copy of this long body rather
 // than one per colour and plaquette slot: the unrolled copies overflowed the
-// instruction cache.
+// instruction cache.  The visit walks the three spin rows mu in turn: it
+// reads row mu of the six neighbours once, forms the gradient terms, draws
+// and forms row mu of the proposal and adds that row's gradient change (and,
+// for the Gaussian, its log density ratio), so only one row of neighbour
+// values is live at a time.  The draws keep the reference's order, which is
+// row by row too.
 //   Cartesian (models/he3/update.py:178-227): twelve offsets, then the
 //     acceptance uniform; potential change plus the exact gradient change.
 //   Conditional Gaussian (gaussian_fast.py:26-119): six Box-Muller pairs, the
@@ -347,80 +366,65 @@ __device__ __noinline__ He3Visit he3_visit(const He3Ctx x, const He3Nbrs n, He3C
     out.accepted = 0;
     out.dE = 0.0f;
     const He3Cell me = *site;
-    if constexpr (!kGauss) {
-        c32 w[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const float re = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
-            const float im = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
-            w[k] = cmk(me.z[k].re + re, me.z[k].im + im);
-        }
-        const float v = mcgb_fast_unit(xoro_next(st));
-        const float dv = he3_potential_f(w, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d);
-        const float diff = dv + x.K * he3_grad_diff(n, me, w);
-        if (diff <= 0.0f || v < __expf(-x.beta * diff)) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) site->z[k] = w[k];
-            out.dE = diff;
-            out.accepted = 1;
-        }
-        out.st = st;
-        return out;
-    } else {
-    c32 zz[6];
-#pragma unroll
-    for (int mu = 0; mu < 3; ++mu) {
-        zz[2 * mu] = he3_normal_pair(st);      // zp
-        zz[2 * mu + 1] = he3_normal_pair(st);  // zm
-    }
-    const float v = mcgb_fast_unit(xoro_next(st));
-    out.st = st;
     const float root = 0.7071067811865475f;
-    const float plus = 10.0f * x.K + x.mass, minus = 6.0f * x.K + x.mass;
-    const float vf = 1.0f - x.rho * x.rho;
-    const float sp = sqrtf(vf / (2.0f * x.beta * plus));
-    const float sm = sqrtf(vf / (2.0f * x.beta * minus));
-    const float qp = vf / (8.0f * root * root * sp * sp);
-    const float qm = vf / (8.0f * root * root * sm * sm);
     c32 nxt[6];
-    float lpr = 0.0f;
+    float dg = 0.0f, lpr = 0.0f;
 #pragma unroll
     for (int mu = 0; mu < 3; ++mu) {
         const int kx = 2 * mu, ky = 2 * mu + 1;
-        const c32 f0 = -3.0f * (n.R->z[kx] + n.Lf->z[kx]) - n.U->z[kx] - n.U->z[ky] - n.R->z[ky] - n.Lf->z[ky] -
-                       n.D->z[kx] - n.D->z[ky] + n.LU->z[ky] + n.DR->z[ky];
-        const c32 f1 = -n.R->z[kx] - n.R->z[ky] - n.U->z[kx] - n.Lf->z[kx] - n.Lf->z[ky] - n.D->z[kx] -
-                       3.0f * (n.U->z[ky] + n.D->z[ky]) + n.LU->z[kx] + n.DR->z[kx];
         const c32 xo = me.z[kx], yo = me.z[ky];
-        const c32 hp = root * (f0 + f1), hm = root * (f0 - f1);
-        c32 mp = (-x.K) * hp, mm = (-x.K) * hm;
-        mp = cmk(mp.re / plus, mp.im / plus);
-        mm = cmk(mm.re / minus, mm.im / minus);
-        const c32 mx = root * (mp + mm), my = root * (mp - mm);
-        const c32 zp = sp * zz[kx], zm = sm * zz[ky];
-        const c32 nx = (mx + x.rho * (xo - mx)) + root * (zp + zm);
-        const c32 ny = (my + x.rho * (yo - my)) + root * (zp - zm);
+        const He3Grad g = he3_grad_terms(n, kx, ky, xo, yo);
+        c32 nx, ny;
+        if constexpr (!kGauss) {
+            const float xr = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
+            const float xi = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
+            const float yr = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
+            const float yi = x.delta * (2.0f * mcgb_fast_unit(xoro_next(st)) - 1.0f);
+            nx = cmk(xo.re + xr, xo.im + xi);
+            ny = cmk(yo.re + yr, yo.im + yi);
+        } else {
+            const c32 f0 = g.fx - (8.0f * xo + 2.0f * yo);
+            const c32 f1 = g.fy - (2.0f * xo + 8.0f * yo);
+            const c32 hp = root * (f0 + f1), hm = root * (f0 - f1);
+            const c32 mp = x.kp * hp, mm = x.km * hm;
+            const c32 mx = root * (mp + mm), my = root * (mp - mm);
+            const c32 zp = x.sp * he3_normal_pair(st);
+            const c32 zm = x.sm * he3_normal_pair(st);
+            nx = (mx + x.rho * (xo - mx)) + root * (zp + zm);
+            ny = (my + x.rho * (yo - my)) + root * (zp - zm);
+            const c32 op = (xo - mx) + (yo - my), om = (xo - mx) - (yo - my);
+            const c32 np = (nx - mx) + (ny - my), nm = (nx - mx) - (ny - my);
+            lpr += x.qp * (norm2(np) - norm2(op));
+            lpr += x.qm * (norm2(nm) - norm2(om));
+        }
+        dg += he3_grad_change(g, nx - xo, ny - yo);
         nxt[kx] = nx;
         nxt[ky] = ny;
-        const c32 op = (xo - mx) + (yo - my), om = (xo - mx) - (yo - my);
-        const c32 np = (nx - mx) + (ny - my), nm = (nx - mx) - (ny - my);
-        lpr += qp * (norm2(np) - norm2(op));
-        lpr += qm * (norm2(nm) - norm2(om));
     }
-    const float dh = he3_potential_f(nxt, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d) +
-                     x.K * he3_grad_diff(n, me, nxt);
-    const float log_ratio = -x.beta * dh + lpr;
-    if (!isfinite(log_ratio)) {
-        if (x.nonfinite) atomicAdd(reinterpret_cast<unsigned long long *>(x.nonfinite), 1ull);
-        return out;
-    }
-    if (log_ratio >= 0.0f || v < __expf(log_ratio)) {
+    const float v = mcgb_fast_unit(xoro_next(st));
+    out.st = st;
+    const float dh = he3_potential_f(nxt, x.coeff, x.g_d) - he3_potential_f(me.z, x.coeff, x.g_d) + x.K * dg;
+    if constexpr (!kGauss) {
+        if (dh <= 0.0f || v < __expf(-x.beta * dh)) {
 #pragma unroll
-        for (int k = 0; k < 6; ++k) site->z[k] = nxt[k];
-        out.dE = dh;
-        out.accepted = 1;
-    }
-    return out;
+            for (int k = 0; k < 6; ++k) site->z[k] = nxt[k];
+            out.dE = dh;
+            out.accepted = 1;
+        }
+        return out;
+    } else {
+        const float log_ratio = -x.beta * dh + lpr;
+        if (!isfinite(log_ratio)) {
+            if (x.nonfinite) atomicAdd(reinterpret_cast<unsigned long long *>(x.nonfinite), 1ull);
+            return out;
+        }
+        if (log_ratio >= 0.0f || v < __expf(log_ratio)) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) site->z[k] = nxt[k];
+            out.dE = dh;
+            out.accepted = 1;
+        }
+        return out;
     }
 }
 
@@ -431,8 +435,14 @@ struct He3Policy {
     static constexpr int kOwnFloats = 0;
     static constexpr int kChannels = 10;
     static constexpr int kSums = 10;  // the last sum is the spin-z density until finish_sample
-    static constexpr int kMaxThreads = 256;  // the visit needs ~250 registers
-    static constexpr int kPairThreads = 256;
+    // The visit walks one spin row at a time and fits 128 registers without
+    // spills, so CTAs of up to 512 threads (16 warps an SM, or two 256-thread
+    // CTAs) run the one-plaquette and global-stream variants.  There is no
+    // two-plaquette variant (kPairThreads = 0): strips with more plaquettes
+    // than threads keep their streams in global memory, whose 32 bytes a
+    // visit are small beside the visit's arithmetic.
+    static constexpr int kMaxThreads = 512;
+    static constexpr int kPairThreads = 0;
     static constexpr bool kSplitMiddle = true;
     static constexpr bool kPipeline = false;  // update<c>: one out-of-line visit
     // Global-stream variant: sites whose visits one thread carries at once.
@@ -452,7 +462,16 @@ struct He3Policy {
         x.delta = a.delta;
         x.g_d = a.g_d;
         x.rho = a.rho;
-        x.mass = a.mass;
+        // gaussian_fast.py:57-66, once per window.
+        const float root = 0.7071067811865475f;
+        const float plus = 10.0f * a.K + a.mass, minus = 6.0f * a.K + a.mass;
+        const float vf = 1.0f - a.rho * a.rho;
+        x.sp = sqrtf(vf / (2.0f * x.beta * plus));
+        x.sm = sqrtf(vf / (2.0f * x.beta * minus));
+        x.qp = vf / (8.0f * root * root * x.sp * x.sp);
+        x.qm = vf / (8.0f * root * root * x.sm * x.sm);
+        x.kp = -a.K / plus;
+        x.km = -a.K / minus;
 #pragma unroll
         for (int q = 0; q < 5; ++q) x.coeff[q] = a.coeff[q];
         x.nonfinite = a.counters ? a.counters + 2 * (size_t)a.n_replicas + r : nullptr;

@@ -403,7 +403,7 @@ class LadderBatch:
             if smem > 232448:
                 continue
             npl_max = max(int(L) ** 2 // (4 * self.effective_cluster(L, C)) for L in Ls)
-            t_max = {MODEL_HE3: 256, MODEL_HE3_GAUSS: 256, MODEL_KAWAMURA: 512,
+            t_max = {MODEL_HE3: 512, MODEL_HE3_GAUSS: 512, MODEL_KAWAMURA: 512,
                      MODEL_KAWAMURA_GAUSS: 512}.get(self.model_id, 1024)
             # Powers of two, and multiples of 96 for sizes whose plaquette
             # counts carry a factor of 3 (L = 48, 96, ...): a thread count
