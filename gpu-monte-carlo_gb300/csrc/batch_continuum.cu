@@ -57,6 +57,9 @@ struct KawamuraPolicy {
     static constexpr bool kSmemStreams = false;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
+    // The cell gathers (cos, sin) from the cache and tau, d from the state:
+    // loaded site by site.
+    static constexpr bool kBulkLoad = false;
 
     struct Ctx {
         float beta, J, delta, sigma;
@@ -450,6 +453,10 @@ struct He3Policy {
     static constexpr bool kSmemStreams = false;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
+
+    // The cell is the site's twelve floats as stored: bulk strip loads.
+    static constexpr bool kBulkLoad = true;
+    static __device__ __forceinline__ const void *bulk_cells(const Args &a) { return a.state; }
 
     using Ctx = He3Ctx;
     struct Prop {};

@@ -39,6 +39,9 @@ struct IsingPolicy {
     static constexpr bool kSmemStreams = true;
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
+    // The strip's int8 spins are the global records: bulk strip loads.
+    static constexpr bool kBulkLoad = true;
+    static __device__ __forceinline__ const void *bulk_cells(const Args &a) { return a.state; }
 
     // u < expf(-beta*dE) for the float32 uniform u of draw x is
     // (x >> 11) < M, with M the integer threshold of that float (exact, see
@@ -134,6 +137,14 @@ struct XYPolicy {
     static constexpr bool kSmemStreams = true;
     static constexpr bool kEnergyFromDelta = true;
     static constexpr bool kExactEnergy = false;
+    // Cells are the (cos, sin) cache and the owner's float the angle, both
+    // stored site by site: bulk strip loads.
+    static constexpr bool kBulkLoad = true;
+    static __device__ __forceinline__ const void *bulk_cells(const Args &a) { return a.aux; }
+    static __device__ __forceinline__ const float *bulk_own(const Args &a)
+    {
+        return static_cast<const float *>(a.state);
+    }
 
     struct Ctx {
         float beta, sigma, J, delta;

@@ -156,6 +156,8 @@ __host__ __device__ constexpr int part_slots()
 // window by the exchange (its lines in the parameter bank go cold over a
 // window's sweeps).
 constexpr size_t kFusedCopyBytes = (sizeof(FusedExchange) + 15) & ~static_cast<size_t>(15);
+// The mbarrier the bulk strip loads complete on (8 bytes, padded to 16).
+constexpr size_t kStripBarBytes = 16;
 
 // Shared memory of a strip with npl plaquettes in rows of lp (with
 // `streams`, also the strip's four colours of RNG streams, 16 B a site).
@@ -163,6 +165,7 @@ template <class M>
 __host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp, bool streams = false)
 {
     return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * part_slots<M>()) + kFusedCopyBytes +
+           kStripBarBytes +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
            (size_t)4 * npl * sizeof(float) * M::kOwnFloats + (streams ? (size_t)4 * npl * 16 + 16 : 0);
 }
@@ -221,6 +224,142 @@ __device__ __forceinline__ void cluster_arrive()
 __device__ __forceinline__ void cluster_wait()
 {
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// Bulk copies (the Blackwell tensor memory accelerator's untiled form,
+// cp.async.bulk) of contiguous strip rows from global into shared memory,
+// completing on an mbarrier that counts the bytes.  Addresses and sizes
+// must be multiples of 16 bytes.
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    // Make the initialisation visible to the async proxy (the copies).
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_addr(dst)),
+        "l"(static_cast<unsigned long long>(__cvta_generic_to_global(src))), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// Orders this thread's earlier shared-memory accesses (generic proxy) before
+// later bulk copies into the same memory (async proxy).
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ bool aligned16(const void *p)
+{
+    return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+}
+
+// Polls of the strip load's mbarrier before a window gives up (each try_wait
+// may itself suspend the thread for a while): far beyond any copy's time.
+constexpr long long kStripWaitLimit = 1ll << 22;
+
+// Whether this CTA's strip can arrive by bulk copies: policies whose
+// shared-memory records are the global records byte for byte (kBulkLoad:
+// M::bulk_cells, and M::bulk_own for the kOwnFloats), each colour's rows one
+// contiguous run in both places, every run starting on 16 bytes with a
+// length that is a multiple of 16.  Uniform over the CTA.
+template <class M, bool SS>
+__device__ __forceinline__ bool strip_bulk_ok(const typename M::Args &a, const typename M::Cell *cells,
+                                              const float *own, const StripCtx &g, int64_t base, int64_t gplane)
+{
+    using Cell = typename M::Cell;
+    if (g.NPL <= 0) return false;
+    const Cell *gc = static_cast<const Cell *>(M::bulk_cells(a));
+    bool ok = ((g.NPL * sizeof(Cell)) & 15u) == 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) ok = ok && aligned16(cells + c * g.PS + g.LP) && aligned16(gc + base + c * gplane);
+    if constexpr (M::kOwnFloats > 0) {
+        const float *go = M::bulk_own(a);
+        ok = ok && ((g.NPL * M::kOwnFloats * sizeof(float)) & 15u) == 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            ok = ok && aligned16(own + (size_t)c * g.NPL * M::kOwnFloats) &&
+                 aligned16(go + (base + c * gplane) * M::kOwnFloats);
+    }
+    return ok;
+}
+
+// The strip by bulk copies: thread 0 issues one copy per colour and array
+// (cells, the owner's floats, and with SS the RNG streams) into rows 1..HP of
+// each haloed plane, completing on `bar`; every thread waits for the bytes
+// (bounded: on giving up, error flag 2 and the window runs on, so no cluster
+// barrier is left waiting), then the boundary rows go to the neighbours'
+// halos as in the per-thread load.  Before the copies, every thread's earlier
+// accesses to these buffers (the previous replica's sweeps and write-back)
+// are ordered before the copies' writes by a proxy fence and a CTA barrier.
+template <class M, bool SS>
+__device__ __forceinline__ void load_strip_bulk(const typename M::Args &a, typename M::Cell *cells, float *own,
+                                                ulonglong2 *sst, const StripCtx &g, int64_t base, int64_t gplane,
+                                                uint64_t *bar, unsigned &phase, int32_t *error)
+{
+    using Cell = typename M::Cell;
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned cb = (unsigned)(g.NPL * sizeof(Cell));
+        const unsigned ob = (unsigned)(g.NPL * M::kOwnFloats * sizeof(float));
+        const unsigned sb = SS ? (unsigned)(g.NPL * sizeof(ulonglong2)) : 0u;
+        mbar_arrive_expect_tx(bar, 4u * (cb + ob + sb));
+        const Cell *gc = static_cast<const Cell *>(M::bulk_cells(a));
+#pragma unroll
+        for (int c = 0; c < 4; ++c) bulk_load(cells + c * g.PS + g.LP, gc + base + c * gplane, cb, bar);
+        if constexpr (M::kOwnFloats > 0) {
+            const float *go = M::bulk_own(a);
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                bulk_load(own + (size_t)c * g.NPL * M::kOwnFloats, go + (base + c * gplane) * M::kOwnFloats, ob,
+                          bar);
+        }
+        if constexpr (SS) {
+            const ulonglong2 *gr = static_cast<const ulonglong2 *>(a.c.rng);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bulk_load(sst + (size_t)c * g.NPL, gr + base + c * gplane, sb, bar);
+        }
+    }
+    for (long long it = 0; !mbar_try_wait(bar, phase); ++it) {
+        if (it >= kStripWaitLimit) {
+            if (threadIdx.x == 0 && error != nullptr) atomicExch(error, 2);
+            break;
+        }
+    }
+    phase ^= 1u;
+    for (int q = threadIdx.x; q < g.LP; q += blockDim.x) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+            *static_cast<Cell *>(__cluster_map_shared_rank(cells + c * g.PS + (g.HP + 1) * g.LP + q, g.up)) =
+                cells[c * g.PS + g.LP + q];
+#pragma unroll
+        for (int c = 2; c < 4; ++c)
+            *static_cast<Cell *>(__cluster_map_shared_rank(cells + c * g.PS + q, g.dn)) =
+                cells[c * g.PS + g.HP * g.LP + q];
+    }
 }
 
 template <class M, int NK, int C_, bool SS = false>
@@ -773,7 +912,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     constexpr int NP = part_slots<M>();
     float2 *parts = reinterpret_cast<float2 *>(scratch + 32 * (NS + 3));  // [kMaxCluster][NP], rank 0's used
     FusedExchange *fxs = reinterpret_cast<FusedExchange *>(parts + kMaxCluster * NP);
-    Cell *cells = reinterpret_cast<Cell *>(reinterpret_cast<unsigned char *>(fxs) + kFusedCopyBytes);
+    uint64_t *strip_bar = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(fxs) + kFusedCopyBytes);
+    Cell *cells = reinterpret_cast<Cell *>(reinterpret_cast<unsigned char *>(strip_bar) + kStripBarBytes);
 
     const WindowCommon &cm = a.c;
     // The work lists hold n_clusters entries for clusters of cluster_size
@@ -788,6 +928,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     }
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
     if (a.fx.enabled && tid == 0) *fxs = a.fx;
+    if (M::kBulkLoad && tid == 0) mbar_init(strip_bar, 1);
+    [[maybe_unused]] unsigned strip_phase = 0;
     // DSMEM stores below need every CTA of the cluster to be running.
     cluster.sync();
 
@@ -808,13 +950,23 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         g.dn = rank + 1 >= Ce ? 0 : rank + 1;
         float *own = reinterpret_cast<float *>(
             (reinterpret_cast<uintptr_t>(cells + 4 * g.PS) + 15) & ~static_cast<uintptr_t>(15));
-        constexpr bool SS = smem_stream_variant<M, NPMAX>();
         [[maybe_unused]] ulonglong2 *sst = reinterpret_cast<ulonglong2 *>(
             (reinterpret_cast<uintptr_t>(own + (size_t)4 * g.NPL * M::kOwnFloats) + 15) & ~static_cast<uintptr_t>(15));
         const int64_t gplane = (int64_t)g.LP * g.LP;
         const int64_t base = rep.state_offset + (int64_t)rank * g.NPL;
 
         // Load the strip; boundary rows also go to the neighbours' halos.
+        // Fused launches (which carry an error flag for the bounded wait)
+        // take bulk copies where the layout allows.
+        constexpr bool SS = smem_stream_variant<M, NPMAX>();
+        bool bulk = false;
+        if constexpr (M::kBulkLoad) {
+            if (a.fx.enabled && strip_bulk_ok<M, SS>(a, cells, own, g, base, gplane)) {
+                bulk = true;
+                load_strip_bulk<M, SS>(a, cells, own, sst, g, base, gplane, strip_bar, strip_phase, a.fx.error);
+            }
+        }
+        if (!bulk)
         for (int c = 0; c < 4; ++c)
             for (int p = tid; p < g.NPL; p += T) {
                 const Site s = make_site(p, g.LP);
@@ -844,8 +996,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
         }
         if constexpr (SS) {
-            for (int c = 0; c < 4; ++c)
-                for (int p = tid; p < g.NPL; p += T) sst[c * g.NPL + p] = rng_g[base + c * gplane + p];
+            if (!bulk)
+                for (int c = 0; c < 4; ++c)
+                    for (int p = tid; p < g.NPL; p += T) sst[c * g.NPL + p] = rng_g[base + c * gplane + p];
         }
         // A resident launch runs n_windows windows with the strip on chip,
         // exchanging between them (each walker waits for its pair's decision

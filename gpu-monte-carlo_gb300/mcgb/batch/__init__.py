@@ -717,18 +717,22 @@ class LadderBatch:
         return int(_lib.load().mcgb_batch_set_wait_limit(-1 if polls is None else int(polls)))
 
     def check_errors(self):
-        """Raise MCGBTimeout if a resident launch gave up waiting between
-        windows.  Its samples and exchange statistics are then unreliable and
-        its slot maps may disagree; before raising, the maps are rebuilt from
-        w2t (identity for a ladder whose w2t is no permutation), the betas
-        set to match and the sync array zeroed, so later runs are sound."""
+        """Raise MCGBTimeout if a fused launch gave up a bounded wait: a
+        resident launch waiting between windows for a pair's decision (flag
+        1) or a window waiting for its strip's bulk copies (flag 2).  Its
+        samples and exchange statistics are then unreliable and its slot maps
+        may disagree; before raising, the maps are rebuilt from w2t (identity
+        for a ladder whose w2t is no permutation), the betas set to match and
+        the sync array zeroed, so later runs are sound."""
         if not self.pt:
             return
-        flag = self.sync.copy_to_host()[-1]
+        flag = int(self.sync.copy_to_host()[-1])
         if flag:
             self._repair_maps()
             self.sync.copy_to_device(np.zeros(len(self.sync), np.int32))
-            raise _lib.MCGBTimeout(-4, "a resident launch timed out waiting between windows")
+            what = ("a window timed out waiting for its strip's bulk copies" if flag == 2
+                    else "a resident launch timed out waiting between windows")
+            raise _lib.MCGBTimeout(-4, what)
 
     def _repair_maps(self):
         w2t = self.w2t.copy_to_host()
