@@ -238,7 +238,14 @@ template <class M>
 int launch_any(const BatchArgs &a, const mcgb_batch_window &w, cudaStream_t s, const char *name)
 {
     MCGB_REQUIRE(w.threads <= M::kMaxThreads, "%s: at most %d threads per CTA", name, M::kMaxThreads);
-    switch (pick_npmax<M>(w)) {
+    const int npmax = pick_npmax<M>(w);
+    if constexpr (M::kRefLayout) {
+        // The reference layout is indexed for the register and shared-memory
+        // stream variants only.
+        MCGB_REQUIRE(npmax == 1 || npmax == 2,
+                     "%s: strips of at most two plaquettes per thread (more CTAs or threads per replica)", name);
+    }
+    switch (npmax) {
     case 1: return launch_window<M, 1>(a, w, s, name);
     case 2:
         if constexpr (M::kPairThreads > 0) return launch_window<M, 2>(a, w, s, name);
@@ -286,7 +293,11 @@ int max_clusters_any(int C, int threads, size_t smem, int *out)
 {
     MCGB_REQUIRE(threads <= M::kMaxThreads, "at most %d threads per CTA for this model", M::kMaxThreads);
     int best = 0, n = 0;
-    if (int st = max_clusters_for<M, 0>(C, threads, smem, &best)) return st;
+    if constexpr (M::kRefLayout) {
+        best = 1 << 30;  // the variants below only
+    } else {
+        if (int st = max_clusters_for<M, 0>(C, threads, smem, &best)) return st;
+    }
     if (threads <= window_max_threads<M, 1>() && (!smem_stream_variant<M, 1>() || smem_streams_fit(smem, threads))) {
         if (int st = max_clusters_for<M, 1>(C, threads, smem, &n)) return st;
         if (n < best) best = n;
@@ -303,7 +314,7 @@ int max_clusters_any(int C, int threads, size_t smem, int *out)
             if (n < best) best = n;
         }
     }
-    *out = best;
+    *out = best == (1 << 30) ? 0 : best;
     return MCGB_OK;
 }
 

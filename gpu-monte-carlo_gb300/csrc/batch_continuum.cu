@@ -59,6 +59,7 @@ struct KawamuraPolicy {
     static constexpr bool kExactEnergy = false;
     // The cell gathers (cos, sin) from the cache and tau, d from the state:
     // loaded site by site.
+    static constexpr bool kRefLayout = false;  // colour-major batch arrays
     static constexpr bool kBulkLoad = false;
 
     struct Ctx {
@@ -455,6 +456,7 @@ struct He3Policy {
     static constexpr bool kExactEnergy = false;
 
     // The cell is the site's twelve floats as stored: bulk strip loads.
+    static constexpr bool kRefLayout = false;  // colour-major batch arrays
     static constexpr bool kBulkLoad = true;
     static __device__ __forceinline__ const void *bulk_cells(const Args &a) { return a.state; }
 

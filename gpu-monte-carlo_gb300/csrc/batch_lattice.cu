@@ -40,6 +40,7 @@ struct IsingPolicy {
     static constexpr bool kEnergyFromDelta = false;
     static constexpr bool kExactEnergy = true;
     // The strip's int8 spins are the global records: bulk strip loads.
+    static constexpr bool kRefLayout = false;  // colour-major batch arrays
     static constexpr bool kBulkLoad = true;
     static __device__ __forceinline__ const void *bulk_cells(const Args &a) { return a.state; }
 
@@ -139,6 +140,7 @@ struct XYPolicy {
     static constexpr bool kExactEnergy = false;
     // Cells are the (cos, sin) cache and the owner's float the angle, both
     // stored site by site: bulk strip loads.
+    static constexpr bool kRefLayout = false;  // colour-major batch arrays
     static constexpr bool kBulkLoad = true;
     static __device__ __forceinline__ const void *bulk_cells(const Args &a) { return a.aux; }
     static __device__ __forceinline__ const float *bulk_own(const Args &a)
@@ -244,6 +246,102 @@ struct XYPolicy {
     static __device__ __forceinline__ double finish_energy(const Ctx &, double e) { return e; }
 };
 
+// ================================================================= reference layout
+//
+// The drop-in Runtime keeps the reference's arrays: (R, L, L) states and
+// one stream per site at r*L*L + i*L + j.  These policies run the window
+// kernel directly on them (strips gathered into colour planes on load,
+// scattered back on write-back), so Simulation runs of the built-in Ising
+// and XY (uniform proposal) models do a whole run of sweeps in one launch
+// with the strip on chip, bit-identical to four update_color launches a
+// sweep: Ising's window decision is already bit-identical to
+// ising_phase_kernel, and XY's uses the same xy_ref_propose/xy_ref_accept
+// as xy_color_kernel.  Windows only: no samples, no fused exchange.
+
+struct IsingRefPolicy : IsingPolicy {
+    static constexpr bool kRefLayout = true;
+    static constexpr bool kBulkLoad = false;
+};
+
+// models/xy/update.py:6-54 on the angles themselves (the cell is theta).
+struct XYRefPolicy {
+    using Args = BatchArgs;
+    using Cell = float;
+    static constexpr int kOwnFloats = 0;
+    static constexpr int kChannels = 5;
+    static constexpr int kSums = 5;
+    static constexpr int kMaxThreads = 1024;
+    static constexpr int kPairThreads = 512;
+    static constexpr bool kSplitMiddle = false;
+    static constexpr bool kPipeline = true;
+    static constexpr int kGlobalInFlight = 1;
+    static constexpr bool kSmemStreams = true;
+    static constexpr bool kEnergyFromDelta = true;
+    static constexpr bool kExactEnergy = false;
+    static constexpr bool kRefLayout = true;
+    static constexpr bool kBulkLoad = false;
+
+    struct Ctx {
+        float beta, J, delta;
+    };
+    struct Prop {
+        float tp, v;
+    };
+
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
+    {
+        return Ctx{__ldcg(a.c.betas + r), a.J, a.delta};
+    }
+    static __device__ __forceinline__ void load(const Args &a, int64_t site, Cell &cell, float *)
+    {
+        cell = static_cast<const float *>(a.state)[site];
+    }
+    static __device__ __forceinline__ void store(const Args &a, int64_t site, const Cell &cell, const float *)
+    {
+        static_cast<float *>(a.state)[site] = cell;
+    }
+    template <int C_>
+    static __device__ __forceinline__ Prop propose(const Ctx &x, const Cell &me, const float *, ulonglong2 &st)
+    {
+        Prop q;
+        q.tp = xy_ref_propose(me, st, x.delta, q.v);
+        return q;
+    }
+    template <int C_>
+    static __device__ __forceinline__ bool decide(const Ctx &x, const Nbrs<Cell> &nb, Cell &me, float *,
+                                                  const Prop &q, float &dE)
+    {
+        if (xy_ref_accept(me, q.tp, q.v, MCGB_NBR(nb, kUp(C_)), MCGB_NBR(nb, kDown(C_)), MCGB_NBR(nb, kLeft(C_)),
+                          MCGB_NBR(nb, kRight(C_)), x.beta, x.J, dE)) {
+            me = q.tp;
+            return true;
+        }
+        return false;
+    }
+    // Samples are not taken in this layout (the drop-in classes measure with
+    // their own kernels); the sums below keep the skeleton complete.
+    template <int C_>
+    static __device__ __forceinline__ void measure(const Ctx &, const Nbrs<Cell> &nb, const Cell &me,
+                                                   const float *, FSum *v)
+    {
+        const float dn = MCGB_NBR(nb, kDown(C_));
+        float s, c, sd, cd;
+        __sincosf(me, &s, &c);
+        __sincosf(me - dn, &sd, &cd);
+        v[1] += c;
+        v[2] += s;
+        v[3] += cd;
+        v[4] += sd;
+    }
+    template <int C_>
+    static __device__ __forceinline__ void energy_site(const Ctx &, const Nbrs<Cell> &, const Cell &,
+                                                       const float *, FSum &)
+    {
+    }
+    static __device__ __forceinline__ void finish_sample(const Ctx &, double *) {}
+    static __device__ __forceinline__ double finish_energy(const Ctx &, double e) { return e; }
+};
+
 // ================================================================= FP64 energies
 
 // Site (i, j) of a colour-major replica.
@@ -311,22 +409,38 @@ int refresh_aux(const mcgb_batch_window &w, int stride, cudaStream_t s)
 int lattice_window(int model, const mcgb_batch_window &w, cudaStream_t s, const FusedExchange *fx)
 {
     if (model == MCGB_MODEL_XY) MCGB_REQUIRE(w.aux != nullptr, "XY window: null (cos, sin) cache");
+    if (model == MCGB_MODEL_ISING_REF || model == MCGB_MODEL_XY_REF)
+        MCGB_REQUIRE(fx == nullptr && w.samples == nullptr,
+                     "reference-layout window: no samples and no fused exchange");
     if (int st = validate_window(w)) return st;
     BatchArgs a = make_args(w);
     if (fx != nullptr) a.fx = *fx;
-    if (model == MCGB_MODEL_ISING) return launch_any<IsingPolicy>(a, w, s, "ising window");
-    return launch_any<XYPolicy>(a, w, s, "xy window");
+    switch (model) {
+    case MCGB_MODEL_ISING: return launch_any<IsingPolicy>(a, w, s, "ising window");
+    case MCGB_MODEL_ISING_REF: return launch_any<IsingRefPolicy>(a, w, s, "ising reference-layout window");
+    case MCGB_MODEL_XY_REF: return launch_any<XYRefPolicy>(a, w, s, "xy reference-layout window");
+    default: return launch_any<XYPolicy>(a, w, s, "xy window");
+    }
 }
 
 int64_t lattice_smem(int model, int L, int C)
 {
-    return (int64_t)(model == MCGB_MODEL_ISING ? single_smem<IsingPolicy>(L, C) : single_smem<XYPolicy>(L, C));
+    switch (model) {
+    case MCGB_MODEL_ISING: return (int64_t)single_smem<IsingPolicy>(L, C);
+    case MCGB_MODEL_ISING_REF: return (int64_t)single_smem<IsingRefPolicy>(L, C);
+    case MCGB_MODEL_XY_REF: return (int64_t)single_smem<XYRefPolicy>(L, C);
+    default: return (int64_t)single_smem<XYPolicy>(L, C);
+    }
 }
 
 int lattice_max_clusters(int model, int C, int threads, size_t smem, int *out)
 {
-    if (model == MCGB_MODEL_ISING) return max_clusters_any<IsingPolicy>(C, threads, smem, out);
-    return max_clusters_any<XYPolicy>(C, threads, smem, out);
+    switch (model) {
+    case MCGB_MODEL_ISING: return max_clusters_any<IsingPolicy>(C, threads, smem, out);
+    case MCGB_MODEL_ISING_REF: return max_clusters_any<IsingRefPolicy>(C, threads, smem, out);
+    case MCGB_MODEL_XY_REF: return max_clusters_any<XYRefPolicy>(C, threads, smem, out);
+    default: return max_clusters_any<XYPolicy>(C, threads, smem, out);
+    }
 }
 
 int lattice_energy64(int model, const mcgb_batch_window &w, double *drift, cudaStream_t s)

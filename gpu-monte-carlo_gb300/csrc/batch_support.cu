@@ -61,8 +61,14 @@ __global__ void tune_sigma_kernel(float *sigma_t, const long long *accepted, lon
 
 using namespace mcgb;
 
-static bool is_lattice(int model) { return model == MCGB_MODEL_ISING || model == MCGB_MODEL_XY; }
-static bool known_model(int model) { return model >= MCGB_MODEL_ISING && model <= MCGB_MODEL_KAWAMURA_GAUSS; }
+static bool is_lattice(int model)
+{
+    return model == MCGB_MODEL_ISING || model == MCGB_MODEL_XY || model == MCGB_MODEL_ISING_REF ||
+           model == MCGB_MODEL_XY_REF;
+}
+static bool known_model(int model) { return model >= MCGB_MODEL_ISING && model <= MCGB_MODEL_XY_REF; }
+// Models of the batch arrays; the reference-layout ones take windows only.
+static bool batch_model(int model) { return model >= MCGB_MODEL_ISING && model <= MCGB_MODEL_KAWAMURA_GAUSS; }
 
 extern "C" int mcgb_batch_channels(int model)
 {
@@ -109,7 +115,7 @@ extern "C" int mcgb_batch_window_run(int model, const mcgb_batch_window *w, void
 
 extern "C" int mcgb_batch_recompute_energy(int model, const mcgb_batch_window *w, double *drift, void *stream)
 {
-    MCGB_REQUIRE(known_model(model), "unknown model %d", model);
+    MCGB_REQUIRE(batch_model(model), "unknown batch model %d", model);
     MCGB_REQUIRE(w && w->table && w->state && w->e_run && w->energies && w->n_replicas >= 1,
                  "recompute_energy: null pointer");
     return is_lattice(model) ? lattice_energy64(model, *w, drift, as_stream(stream))
@@ -158,7 +164,7 @@ extern "C" int mcgb_batch_exchange(const mcgb_batch_window *w, const mcgb_batch_
 extern "C" int mcgb_batch_window_exchange(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                           int32_t *sync, void *stream)
 {
-    MCGB_REQUIRE(known_model(model), "unknown model %d", model);
+    MCGB_REQUIRE(batch_model(model), "unknown batch model %d", model);
     MCGB_REQUIRE(w && pt, "window_exchange: null argument block");
     MCGB_REQUIRE(sync != nullptr, "window_exchange: null sync counters");
     if (int st = check_exchange(*w, *pt)) return st;
@@ -184,7 +190,7 @@ extern "C" int64_t mcgb_batch_set_wait_limit(int64_t polls)
 extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_batch_pt *pt,
                                        int32_t *sync, int n_windows, void *stream)
 {
-    MCGB_REQUIRE(known_model(model), "unknown model %d", model);
+    MCGB_REQUIRE(batch_model(model), "unknown batch model %d", model);
     MCGB_REQUIRE(w && pt, "run_resident: null argument block");
     MCGB_REQUIRE(sync != nullptr, "run_resident: null sync counters");
     MCGB_REQUIRE(n_windows >= 1, "run_resident: n_windows must be >= 1");

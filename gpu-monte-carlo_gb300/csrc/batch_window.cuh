@@ -184,6 +184,23 @@ struct StripCtx {
     int LP, HP, NPL, PS, up, dn;
 };
 
+// Global index of plaquette p of colour c in the strip of CTA `rank`:
+// colour-major (base + c * gplane + p, base = state_offset + rank * NPL), or,
+// for a policy with kRefLayout, the reference layout, site (i, j) of the
+// replica at state_offset + i * L + j (streams in the same order).
+template <class M>
+__device__ __forceinline__ int64_t strip_site(const mcgb_replica &rep, const StripCtx &g, int rank, int64_t base,
+                                              int64_t gplane, int c, int p)
+{
+    if constexpr (M::kRefLayout) {
+        const int pr = p / g.LP, pc = p - pr * g.LP;
+        const int i = 2 * (rank * g.HP + pr) + (c >> 1), j = 2 * pc + (c & 1);
+        return rep.state_offset + (int64_t)i * rep.L + j;
+    } else {
+        return base + c * gplane + p;
+    }
+}
+
 // CTAs of a C-CTA cluster that hold a replica of size L: the largest divisor
 // of L/2 (the plaquette rows) that does not exceed C.  The other CTAs of the
 // cluster hold no rows of that replica and only take part in the barriers,
@@ -971,7 +988,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             for (int p = tid; p < g.NPL; p += T) {
                 const Site s = make_site(p, g.LP);
                 Cell &me = cells[c * g.PS + s.o + s.pc];
-                M::load(a, base + c * gplane + p, me, own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
+                M::load(a, strip_site<M>(rep, g, rank, base, gplane, c, p), me,
+                        own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
                 if (c < 2 && s.pr == 0)
                     *static_cast<Cell *>(
                         __cluster_map_shared_rank(cells + c * g.PS + (g.HP + 1) * g.LP + s.pc, g.up)) = me;
@@ -992,13 +1010,14 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             if (regs && !SS) {
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    if (p < g.NPL) st[k][c] = rng_g[base + c * gplane + p];
+                    if (p < g.NPL) st[k][c] = rng_g[strip_site<M>(rep, g, rank, base, gplane, c, p)];
             }
         }
         if constexpr (SS) {
             if (!bulk)
                 for (int c = 0; c < 4; ++c)
-                    for (int p = tid; p < g.NPL; p += T) sst[c * g.NPL + p] = rng_g[base + c * gplane + p];
+                    for (int p = tid; p < g.NPL; p += T)
+                        sst[c * g.NPL + p] = rng_g[strip_site<M>(rep, g, rank, base, gplane, c, p)];
         }
         // A resident launch runs n_windows windows with the strip on chip,
         // exchanging between them (each walker waits for its pair's decision
@@ -1174,19 +1193,20 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         for (int c = 0; c < 4; ++c)
             for (int p = tid; p < g.NPL; p += T) {
                 const Site s = make_site(p, g.LP);
-                M::store(a, base + c * gplane + p, cells[c * g.PS + s.o + s.pc],
+                M::store(a, strip_site<M>(rep, g, rank, base, gplane, c, p), cells[c * g.PS + s.o + s.pc],
                          own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
             }
         if constexpr (SS) {
             for (int c = 0; c < 4; ++c)
-                for (int p = tid; p < g.NPL; p += T) rng_g[base + c * gplane + p] = sst[c * g.NPL + p];
+                for (int p = tid; p < g.NPL; p += T)
+                    rng_g[strip_site<M>(rep, g, rank, base, gplane, c, p)] = sst[c * g.NPL + p];
         } else if (regs) {
 #pragma unroll
             for (int k = 0; k < NK; ++k) {
                 const int p = tid + k * T;
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    if (p < g.NPL) rng_g[base + c * gplane + p] = st[k][c];
+                    if (p < g.NPL) rng_g[strip_site<M>(rep, g, rank, base, gplane, c, p)] = st[k][c];
             }
         }
         }

@@ -11,6 +11,7 @@
 // in the reference kernels.  Reductions accumulate in float64 with one
 // thread-block cluster per replica (warp shuffles, a pass over warp sums,
 // then the CTAs' sums in rank order through distributed shared memory).
+#include "ffmath.h"
 #include "mcgb_common.cuh"
 
 namespace mcgb {
@@ -142,12 +143,15 @@ __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restric
     ulonglong2 st = rng[idx];
     float proposed, v;
     if (!kGauss) {
-        const float u = xoro_uniform_f32(st);
-        proposed = th + delta * (2.0f * u - 1.0f);
-        // delta <= pi and theta in [-pi, pi): one wrap suffices.
-        if (proposed >= pi) proposed -= two_pi;
-        else if (proposed < -pi) proposed += two_pi;
-        v = xoro_uniform_f32(st);
+        // The reference's rule, shared with the reference-layout window.
+        proposed = xy_ref_propose(th, st, delta, v);
+        const int up = wrapi(i - 1, L) * L + j, down = wrapi(i + 1, L) * L + j;
+        const int left = i * L + wrapi(j - 1, L), right = i * L + wrapi(j + 1, L);
+        float dE;
+        const bool acc = xy_ref_accept(th, proposed, v, b[up], b[down], b[left], b[right], betas[r], J, dE);
+        rng[idx] = st;
+        if (acc) b[i * L + j] = proposed;
+        return;
     } else {
         // One draw per visit: u1, u2 and the acceptance v (mcgb_visit_*).
         const uint64_t x = xoro_next(st);
@@ -205,6 +209,13 @@ __global__ void xy64_color_kernel(double *__restrict__ theta, ulonglong2 *__rest
 }
 
 // models/xy/measure.py:17-134.  NC = 1: energy only; NC = 5: all channels.
+// The reference evaluates cos and sin of every bond angle and spin angle in
+// float64.  GB300's float64 pipe issues a small fraction of the float32
+// rate, so the terms come from float-float arithmetic on the float32 pipe
+// (ff_sincos of the exact float-float difference of two float angles, error
+// below 1e-14) and accumulate per thread as float-float; only the per-thread
+// totals enter the float64 cluster reduction.  The result differs from a
+// float64 evaluation by about 1e-14 per term.
 template <int NC>
 __global__ void xy_reduce_kernel(const float *__restrict__ theta, int R, int L, float J,
                                  const int32_t *__restrict__ tidx, const double *__restrict__ cached,
@@ -214,31 +225,33 @@ __global__ void xy_reduce_kernel(const float *__restrict__ theta, int R, int L, 
     const ReplicaSpan sp = replica_span();
     const int r = sp.r;
     const float *b = theta + (int64_t)r * L * L;
-    double v[NC];
+    ff acc[NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) v[c] = 0.0;
+    for (int c = 0; c < NC; ++c) acc[c] = ff_make(0.0f, 0.0f);
     const bool need_e = cached == nullptr;
     for (int k = sp.first; k < L * L; k += sp.step) {
         const int i = k / L, j = k - i * L;
-        const double t = b[k];
-        const double dx = t - (double)b[wrapi(i + 1, L) * L + j];
-        // cos and sin of the x-bond angle from one argument reduction when
-        // both are needed (the float64 pipe is the bound of this kernel).
-        double cos_x, sin_x = 0.0;
-        if (NC == 5)
-            sincos(dx, &sin_x, &cos_x);
-        else
-            cos_x = cos(dx);
-        if (need_e) v[0] += -(double)J * (cos_x + cos(t - (double)b[i * L + wrapi(j + 1, L)]));
+        const float t = b[k];
+        ff sin_x, cos_x;
+        ff_sincos(ff_diff(t, b[wrapi(i + 1, L) * L + j]), &sin_x, &cos_x);
+        if (need_e) {
+            ff sin_y, cos_y;
+            ff_sincos(ff_diff(t, b[i * L + wrapi(j + 1, L)]), &sin_y, &cos_y);
+            acc[0] = ff_add(acc[0], ff_add(cos_x, cos_y));
+        }
         if (NC == 5) {
-            double sn, cs;
-            sincos(t, &sn, &cs);
-            v[NC == 5 ? 1 : 0] += cs;
-            v[NC == 5 ? 2 : 0] += sn;
-            v[NC == 5 ? 3 : 0] += cos_x;
-            v[NC == 5 ? 4 : 0] += sin_x;
+            ff sn, cs;
+            ff_sincos(ff_make(t, 0.0f), &sn, &cs);
+            acc[NC == 5 ? 1 : 0] = ff_add(acc[NC == 5 ? 1 : 0], cs);
+            acc[NC == 5 ? 2 : 0] = ff_add(acc[NC == 5 ? 2 : 0], sn);
+            acc[NC == 5 ? 3 : 0] = ff_add(acc[NC == 5 ? 3 : 0], cos_x);
+            acc[NC == 5 ? 4 : 0] = ff_add(acc[NC == 5 ? 4 : 0], sin_x);
         }
     }
+    double v[NC];
+    v[0] = -(double)J * ff_to_double(acc[0]);
+#pragma unroll
+    for (int c = 1; c < NC; ++c) v[c] = ff_to_double(acc[c]);
     cluster_sum<NC>(v, scratch, part);
     if (sp.rank == 0 && threadIdx.x == 0) {
         const int d = tidx ? tidx[r] : r;

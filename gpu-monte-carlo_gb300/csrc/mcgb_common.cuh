@@ -62,6 +62,47 @@ __device__ __forceinline__ float xoro_uniform_f32(ulonglong2 &s)
     return mcgb_unit_f32(xoro_next(s));
 }
 
+// ---------------------------------------------------------------- XY visit (reference arithmetic)
+//
+// models/xy/update.py:19-54 in two halves, shared by the per-colour kernel
+// and the reference-layout window so both produce the same bits.  Every
+// float32 operation is rounded on its own (the __f*_rn intrinsics are never
+// contracted into fused multiply-adds), as in the reference's arithmetic.
+
+// The proposal theta + delta (2u - 1), wrapped once into [-pi, pi) (delta <=
+// pi and theta in [-pi, pi)), and the acceptance uniform v, in the
+// reference's draw order.
+__device__ __forceinline__ float xy_ref_propose(float th, ulonglong2 &st, float delta, float &v)
+{
+    const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
+    const float u = xoro_uniform_f32(st);
+    float p = __fadd_rn(th, __fmul_rn(delta, __fsub_rn(__fmul_rn(2.0f, u), 1.0f)));
+    if (p >= pi)
+        p = __fsub_rn(p, two_pi);
+    else if (p < -pi)
+        p = __fadd_rn(p, two_pi);
+    v = xoro_uniform_f32(st);
+    return p;
+}
+
+// -J times the bond cosines of angle t with its four neighbours, in the
+// reference's order (up, down, left, right).
+__device__ __forceinline__ float xy_ref_site_energy(float t, float up, float down, float left, float right, float J)
+{
+    const float c = __fadd_rn(__fadd_rn(__fadd_rn(cosf(__fsub_rn(t, up)), cosf(__fsub_rn(t, down))),
+                                        cosf(__fsub_rn(t, left))),
+                              cosf(__fsub_rn(t, right)));
+    return __fmul_rn(-J, c);
+}
+
+// The Metropolis decision of proposal p for angle th; dE the energy change.
+__device__ __forceinline__ bool xy_ref_accept(float th, float p, float v, float up, float down, float left,
+                                              float right, float beta, float J, float &dE)
+{
+    dE = __fsub_rn(xy_ref_site_energy(p, up, down, left, right, J), xy_ref_site_energy(th, up, down, left, right, J));
+    return dE <= 0.0f || v < expf(__fmul_rn(-beta, dE));
+}
+
 // ---------------------------------------------------------------- complex64
 
 struct c32 {

@@ -99,6 +99,7 @@ class Runtime:
         self.betas = to_device((1.0 / self.temperatures).astype(np.float32))
         self.threads_per_block, self.blocks_per_grid = launch_shape(L, self.R, threads)
         self._energy = EnergyCache()
+        self._window = None  # the window launch of _enqueue_sweeps, built on first use
 
     # ------------------------------------------------------------ energies
     def invalidate_energy_cache(self):
@@ -136,6 +137,26 @@ class Runtime:
         for colour in range(4):
             self.model.update_color(self.state, self.rng_states, self.betas, colour,
                                     self.blocks_per_grid, self.threads_per_block)
+
+    def _enqueue_sweeps(self, n):
+        """The device work of n consecutive sweeps with nothing between them:
+        for the built-in Ising plugin and the XY plugin with the reference's
+        uniform proposal one window launch with the lattice on chip
+        (window_sweeps.py), bit-identical to n sweeps of colour launches;
+        otherwise n times _enqueue_sweep."""
+        self._prepare_sweeps()
+        if self._window:
+            self._window.enqueue(n)
+            return
+        for _ in range(n):
+            self._enqueue_sweep()
+
+    def _prepare_sweeps(self):
+        """Build the window launch of _enqueue_sweeps (its device tables are
+        copied in synchronously, so this must run before any stream capture)."""
+        if self._window is None:
+            from .window_sweeps import WindowSweeps
+            self._window = WindowSweeps.for_runtime(self) or False
 
     def _sweeps_done(self, n):
         """Host bookkeeping, other than the energy cache, after n sweeps whose

@@ -155,8 +155,7 @@ class GraphReplay:
     # ------------------------------------------------------------ device work
     def _enqueue(self, seg, ctx):
         rt, pt = self.rt, self.pt
-        for _ in range(seg.sweeps):
-            rt._enqueue_sweep()
+        rt._enqueue_sweeps(seg.sweeps)
         if seg.exchange:
             pt._enqueue_exchange(ctx["clock"], seg.advance)
             if seg.record:
@@ -173,6 +172,7 @@ class GraphReplay:
         """Enqueue the whole plan, account for it on the host, and return the
         samples {channel: (n_samples, R) float64} in temperature order."""
         rt, pt = self.rt, self.pt
+        rt._prepare_sweeps()  # device tables of the sweep launch, before any capture
         names = tuple(rt.model.measurement_names)
         C, R = len(names), rt.R
         n_samples = len(p.sample_sweeps)

@@ -298,6 +298,16 @@ enum {
     MCGB_MODEL_HE3_GAUSS = 4, /* conditional Gaussian MH proposals */
     MCGB_MODEL_KAWAMURA_GAUSS = 5, /* Gaussian MH proposals (theta and d), widths sigma_t;
                                       no reference counterpart */
+    /* Windows over replicas stored in the reference layout instead: (R, L, L)
+     * states, the stream of site (i, j) of replica r at r*L*L + i*L + j, one
+     * replica of size L per table entry with state_offset = r*L*L.  Only
+     * mcgb_batch_smem_bytes, mcgb_batch_max_clusters and mcgb_batch_window_run
+     * take them, without samples; every strip must hold at most two
+     * plaquettes per thread.  The sweeps are bit-identical to four
+     * mcgb_ising_update_color / mcgb_xy_update_color (uniform proposal)
+     * launches each (models/ising/update.py:7-29, models/xy/update.py:6-54). */
+    MCGB_MODEL_ISING_REF = 6,
+    MCGB_MODEL_XY_REF = 7,
 };
 
 typedef struct mcgb_replica {
