@@ -793,6 +793,7 @@ def run_workload(args, rank, world):
                    "cluster_size": batch.cluster_size, "threads": batch.threads,
                    "size_groups": [{"L": sizes, "cluster_size": c, "threads": t, "resident": r}
                                    for sizes, c, t, r in batch.shapes()] if len(batch.groups) > 1 else None,
+                   "size_groups_side_by_side": bool(batch.concurrent) if len(batch.groups) > 1 else None,
                    "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": f"independent ladders x{world}"},
         "e2e": {"value": e2e_value, "unit": "updates/ns", "h2d_bytes_per_step": int(h2d),

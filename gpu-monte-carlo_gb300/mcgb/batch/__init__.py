@@ -143,6 +143,10 @@ class _Group:
         self.cluster_size = self.threads = self.n_clusters = 0
         self.work_ptr = self.work_idx = self.work_host = None
         self.resident = False
+        # Concurrent groups: the group's stream, its copy of the clock and
+        # its own exchange bookkeeping (mailboxes, decision words, launch
+        # counter, error flag).
+        self.stream = self.clock = self.sync = None
 
 
 def _validate_ladder(L, temperatures, pt):
@@ -179,6 +183,9 @@ class LadderBatch:
         self.model = model
         self._resident_wanted = bool(resident)
         self._resident_checked = False
+        # Size groups launched side by side on streams of their own (set by
+        # split_by_size or autotune); otherwise one after another.
+        self.concurrent = False
         self.model_id, self.dtype, self.site_shape = _model_info(model, gaussian, proposal)
         self.channels = CHANNELS[self.model_id]
         self.pt = exchange_interval is not None
@@ -474,18 +481,68 @@ class LadderBatch:
         g.work_ptr, g.work_idx = to_device(wp), to_device(g.work_host)
         # Resident launches (many windows per launch, strips kept on chip)
         # need one replica per cluster and every cluster resident at once.
+        # Concurrent groups share the GPU, so no group runs cooperative
+        # (resident) launches then.
         g.resident = (self._resident_wanted and self.pt and g.n_clusters == len(idx)
-                      and bool(np.all(np.diff(wp) == 1)))
+                      and bool(np.all(np.diff(wp) == 1)) and not self._side_by_side())
 
-    def split_by_size(self, split=True):
+    def split_by_size(self, split=True, concurrent=False):
         """One group -- one launch per window, its own cluster shape -- per
-        lattice size (split=True), or one group for the whole batch."""
+        lattice size (split=True), or one group for the whole batch.  With
+        `concurrent` the groups' launches of a window run side by side on
+        streams of their own, each from its own copy of the device clock and
+        with its own exchange bookkeeping (a ladder never spans groups), and
+        the step continues once all have finished; otherwise one after
+        another on the current stream."""
         Ls = self.table_host["L"]
         if split:
             self.groups = [_Group(np.flatnonzero(Ls == L)) for L in np.unique(Ls)]
         else:
             self.groups = [_Group(np.arange(self.R))]
+        self.concurrent = bool(concurrent) and split
+        self._graphs.clear()
         self.configure()
+
+    def _side_by_side(self):
+        return self.concurrent and len(self.groups) > 1
+
+    def _group_resources(self):
+        for g in self.groups:
+            if g.stream is None:
+                g.stream = torch.cuda.Stream()
+                g.clock = device_zeros(2, np.int64)
+                if self.pt:
+                    g.sync = device_zeros(len(self.sync), np.int32)
+
+    def _syncs(self):
+        """Every exchange-bookkeeping array in use."""
+        if not self.pt:
+            return []
+        return [self.sync] + [g.sync for g in self.groups if g.sync is not None]
+
+    def _side_by_side_launch(self, launch, take_group_clock):
+        """launch(g, stream handle) for every group on the group's stream,
+        forked from and joined back into the current stream (so a CUDA graph
+        captures the fork and the join).  Each group starts from a copy of
+        the clock; with take_group_clock the groups advanced their copies
+        (all by the same windows) and the batch clock takes group 0's."""
+        self._group_resources()
+        main = torch.cuda.current_stream()
+        fork = torch.cuda.Event()
+        fork.record(main)
+        joins = []
+        for g in self.groups:
+            g.stream.wait_event(fork)
+            with torch.cuda.stream(g.stream):
+                g.clock.raw().copy_(self.clock.raw())
+                launch(g, _lib.stream_handle())
+                done = torch.cuda.Event()
+                done.record(g.stream)
+                joins.append(done)
+        for done in joins:
+            main.wait_event(done)
+        if take_group_clock:
+            self.clock.raw().copy_(self.groups[0].clock.raw())
 
     # The first group's shape (the only group unless the batch is split).
     @property
@@ -526,7 +583,7 @@ class LadderBatch:
         return [([int(L) for L in self._sizes(g.idx)], g.cluster_size, g.threads, g.resident) for g in self.groups]
 
     # ------------------------------------------------------------ argument blocks
-    def _window(self, n_sweeps, staging=False, group=None):
+    def _window(self, n_sweeps, staging=False, group=None, clock=None):
         g = self.groups[0] if group is None else group
         w = BatchWindow()
         w.table = self.table.ptr
@@ -548,7 +605,7 @@ class LadderBatch:
             w.n_slots = self.n_slots
             w.first_sample_sweep = self.first_sample_sweep
             w.sample_interval = self.sample_interval
-        w.clock = self.clock.ptr
+        w.clock = self.clock.ptr if clock is None else clock.ptr
         w.n_sweeps = int(n_sweeps)
         w.J = float(getattr(self.model, "J", 1.0))
         w.delta = float(getattr(self.model, "delta", 0.0))
@@ -573,6 +630,25 @@ class LadderBatch:
     # ------------------------------------------------------------ stepping
     def _enqueue_window(self, n_sweeps, exchange, tune=False):
         s = _lib.stream_handle()
+        if self._side_by_side() and not tune:
+            p = self._pt() if exchange else None
+            self._keep_pt, keep = p, []
+
+            def launch(g, gs):
+                w = self._window(n_sweeps, staging=exchange, group=g, clock=g.clock)
+                keep.append(w)
+                if exchange:
+                    # Window, exchange and the group clock's tick in one launch.
+                    _lib.call("mcgb_batch_window_exchange", self.model_id, ctypes.byref(w), ctypes.byref(p),
+                              g.sync.cptr, gs)
+                else:
+                    _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), gs)
+
+            self._side_by_side_launch(launch, take_group_clock=exchange)
+            self._keep = keep
+            if not exchange:
+                _lib.call("mcgb_batch_clock_tick", self.clock.cptr, int(n_sweeps), 0, s)
+            return
         if exchange and not tune:
             # Window, exchange and clock tick in one launch per group (the
             # last group's launch advances the clock).
@@ -659,6 +735,19 @@ class LadderBatch:
         s = _lib.stream_handle()
         p = self._pt()
         self._keep_pt = p
+        if self._side_by_side():
+            keep = []
+
+            def launch(g, gs):
+                for _ in range(count):
+                    w = self._window(n_sweeps, staging=True, group=g, clock=g.clock)
+                    keep.append(w)
+                    _lib.call("mcgb_batch_window_exchange", self.model_id, ctypes.byref(w), ctypes.byref(p),
+                              g.sync.cptr, gs)
+
+            self._side_by_side_launch(launch, take_group_clock=True)
+            self._keep = keep
+            return
         res = [g for g in self.groups if g.resident]
         non = [g for g in self.groups if not g.resident]
         for i, g in enumerate(res):
@@ -693,7 +782,7 @@ class LadderBatch:
             self._graphs.clear()
             self._advance(step[0], step[1], count)
             return
-        key = (count, step, tune, self.samples is not None and self.samples.ptr, resident)
+        key = (count, step, tune, self.samples is not None and self.samples.ptr, resident, self._side_by_side())
         g = self._graphs.get(key)
         if g is None:
             # Capture reads only argument blocks; the device clock advances at replay.
@@ -726,10 +815,11 @@ class LadderBatch:
         the sync array zeroed, so later runs are sound."""
         if not self.pt:
             return
-        flag = int(self.sync.copy_to_host()[-1])
+        flag = max(int(sy.copy_to_host()[-1]) for sy in self._syncs())
         if flag:
             self._repair_maps()
-            self.sync.copy_to_device(np.zeros(len(self.sync), np.int32))
+            for sy in self._syncs():
+                sy.copy_to_device(np.zeros(len(sy), np.int32))
             what = ("a window timed out waiting for its strip's bulk copies" if flag == 2
                     else "a resident launch timed out waiting between windows")
             raise _lib.MCGBTimeout(-4, what)
@@ -969,14 +1059,21 @@ class LadderBatch:
             # step replays graphs of resident launches, which hide most of
             # that cost.  So the grouping is chosen on a few real steps.
             many_run = self._time_steps(n)
+            # The same groups launched side by side on streams of their own.
+            self.split_by_size(True, concurrent=True)
+            for g, (C, T) in zip(self.groups, many_shapes):
+                self._configure_group(g, C, T)
+            side_run = self._time_steps(n)
             self.split_by_size(False)
             self.configure(*one_shape)
             one_run = self._time_steps(n)
             if verbose:
                 print(f"autotune: one launch {one:.3f} ms, one per size {many:.3f} ms per {n}-sweep window "
-                      f"(trials); {one_run:.3f} ms against {many_run:.3f} ms (steps)")
-            if many_run < 0.98 * one_run:
-                self.split_by_size(True)
+                      f"(trials); {one_run:.3f} ms against {many_run:.3f} ms one after another and "
+                      f"{side_run:.3f} ms side by side (steps)")
+            best = min(many_run, side_run)
+            if best < 0.98 * one_run:
+                self.split_by_size(True, concurrent=side_run < many_run)
                 for g, (C, T) in zip(self.groups, many_shapes):
                     self._configure_group(g, C, T)
                 self._graphs.clear()
@@ -986,7 +1083,7 @@ class LadderBatch:
                 results = one_trials
         else:
             if split is not None and ragged and split != (len(self.groups) > 1):
-                self.split_by_size(split)
+                self.split_by_size(split, concurrent=self.concurrent)
             _, results = tune_groups()
         self.state.raw().copy_(saved_state)
         if saved_aux is not None:
@@ -1027,7 +1124,8 @@ class LadderBatch:
         if self.pt:
             # decision words of the rounds just run would match the same
             # rounds run again
-            self.sync.copy_to_device(np.zeros(len(self.sync), np.int32))
+            for sy in self._syncs():
+                sy.copy_to_device(np.zeros(len(sy), np.int32))
         self._graphs.clear()
         self._resident_checked = False
         return ms

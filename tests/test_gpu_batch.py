@@ -80,14 +80,17 @@ def test_ising_batch_pt_simulation_equals_dropin_simulation(L2, split):
         np.testing.assert_array_equal(b.ladder_state(k), rt.snapshot())
 
 
-@pytest.mark.parametrize("resident,split", [(True, False), (False, False), (True, True), (False, True)])
+@pytest.mark.parametrize("resident,split", [(True, False), (False, False), (True, True), (False, True),
+                                            (True, "side"), (False, "side")])
 def test_graph_replay_equals_direct_launches(resident, split):
     """Replayed graphs (resident: ten windows per launch, each walker waiting
     for its own pair only; split: one launch per lattice size, each with its
-    own cluster shape, the last advancing the clock) against one fused launch
-    per window over the whole batch, on ragged ladders with unpaired end
-    slots and a two-slot ladder: identical chains, maps, betas, swap and
-    round-trip counters, samples and clock."""
+    own cluster shape, the last advancing the clock; "side": the per-size
+    launches side by side on streams of their own, each advancing its own
+    copy of the clock, never resident) against one fused launch per window
+    over the whole batch, on ragged ladders with unpaired end slots and a
+    two-slot ladder: identical chains, maps, betas, swap and round-trip
+    counters, samples and clock."""
     from mcgb.batch import LadderBatch
     from mcgb.models.xy.model import XYModel
     ladders = [(32, np.geomspace(0.7, 1.2, 6)), (16, [0.8, 1.0]), (16, [0.7, 0.9, 1.1])]
@@ -95,9 +98,9 @@ def test_graph_replay_equals_direct_launches(resident, split):
     a = LadderBatch(XYModel(), ladders, resident=resident, **kw)
     c = LadderBatch(XYModel(), ladders, resident=False, **kw)
     if split:
-        a.split_by_size(True)
+        a.split_by_size(True, concurrent=split == "side")
         assert [sizes for sizes, *_ in a.shapes()] == [[16], [32]]
-    assert a.resident == resident
+    assert a.resident == (resident and split != "side")
     for b in (a, c):
         b.allocate_samples(5, 5, 12)
     a.run(60, graph=True)
