@@ -737,23 +737,23 @@ def run_workload(args, rank, world):
     # The window kernel alone (one window of the schedule, samples on).
     from mcgb.batch import NO_EXCHANGE_WINDOW
     win = ex or NO_EXCHANGE_WINDOW
-    ws = [batch._window(win, group=g) for g in batch.groups]  # one launch per size group
-    for w in ws:
-        _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+    # One launch per size group, side by side when the batch runs its groups so.
+    batch.enqueue_plain_windows(win)
     torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record(stream)
     for _ in range(10):
-        for w in ws:
-            _lib.call("mcgb_batch_window_run", batch.model_id, ctypes.byref(w), _lib.stream_handle())
+        batch.enqueue_plain_windows(win)
     k1.record(stream)
     torch.cuda.synchronize()
     window_ms = k0.elapsed_time(k1) / 10
     sm_mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
     prof = PROFILE.get(args.workload)
     roofline = roofline_line(profile_figures(prof), prof, n_sites * win, window_ms, BYTES[kind], sm_mhz,
-                             f"window_kernel ({kind})" + (f", {len(ws)} launches (size groups)" if len(ws) > 1
-                                                          else ""), scale_traffic=True)
+                             f"window_kernel ({kind})" + (
+                                 f", {len(batch.groups)} launches (size groups"
+                                 + (", side by side)" if batch.concurrent else ")") if len(batch.groups) > 1
+                                 else ""), scale_traffic=True)
 
     # End to end: the chain state up from pinned memory, 100 sweeps, the
     # chain state and the step's samples back.

@@ -675,6 +675,27 @@ class LadderBatch:
             _lib.call("mcgb_batch_exchange", ctypes.byref(w), ctypes.byref(p), s)
         _lib.call("mcgb_batch_clock_tick", self.clock.cptr, int(n_sweeps), int(bool(exchange)), s)
 
+    def enqueue_plain_windows(self, n_sweeps):
+        """One window of n_sweeps sweeps of every group, without exchange or
+        clock tick, side by side when the groups run so: the window kernels
+        alone, as a benchmark times them (the chain advances)."""
+        if self._side_by_side():
+            keep = []
+
+            def launch(g, gs):
+                w = self._window(n_sweeps, group=g, clock=g.clock)
+                keep.append(w)
+                _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), gs)
+
+            self._side_by_side_launch(launch, take_group_clock=False)
+            self._keep = keep
+            return
+        s = _lib.stream_handle()
+        for g in self.groups:
+            w = self._window(n_sweeps, group=g)
+            self._keep = w
+            _lib.call("mcgb_batch_window_run", self.model_id, ctypes.byref(w), s)
+
     def _schedule(self, n_sweeps):
         """Split n_sweeps into (length, exchange_after) windows aligned to the PT schedule."""
         out = []
