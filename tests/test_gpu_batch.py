@@ -46,10 +46,12 @@ def test_ising_batch_bit_exact_with_dropin_runtime(cluster_size, threads):
         np.testing.assert_array_equal(e[k], oracle.ising_energy(b.ladder_state(k), np.float32(1))[0])
 
 
-@pytest.mark.parametrize("L2,split", [(16, False), (24, True)])
+@pytest.mark.parametrize("L2,split", [(16, False), (24, True), (64, False), (64, True)])
 def test_ising_batch_pt_simulation_equals_dropin_simulation(L2, split):
     """Same seeds: identical samples, maps and swap counters to Simulation(ParallelTempering),
-    also with the ladders of two sizes run as one launch per size."""
+    also with the ladders of two sizes run as one launch per size.  The 64^2
+    ladder's strips (512-byte colour rows, 16-byte aligned) arrive by bulk
+    copies in the fused launches; the 16^2 and 24^2 ones by per-thread loads."""
     from mcgb.batch import LadderBatch
     from mcgb.core.parallel_tempering import ParallelTempering
     from mcgb.core.runtime import Runtime
@@ -609,3 +611,25 @@ def test_autotune_of_a_ragged_batch_times_real_steps_and_puts_everything_back():
     for name in ("w2t", "t2w", "betas", "swap_counts", "trips", "energies", "clock", "samples"):
         np.testing.assert_array_equal(getattr(a, name).copy_to_host(), getattr(b, name).copy_to_host(), err_msg=name)
     assert a.sweeps == b.sweeps == 40 and a.exchange_rounds == b.exchange_rounds == 8
+
+
+def test_bulk_strip_loads_equal_per_thread_loads():
+    """XY ladder of 128^2 replicas in the shared-memory stream variant (4 CTAs
+    x 1024 threads): fused window + exchange launches, whose strips, angles
+    and streams arrive by bulk copies, against the window-only launches
+    with per-thread loads followed by the separate exchange kernel (the
+    warm-up path): identical chains, streams, maps, counters and energies."""
+    from mcgb.batch import LadderBatch
+    from mcgb.models.xy.model import XYModel
+    temps = np.geomspace(0.7, 1.2, 4)
+    init = np.random.default_rng(31).uniform(-np.pi, np.pi, (4, 128, 128)).astype(np.float32)
+    kw = dict(seeds=[9], exchange_interval=5, cluster_size=4, threads=1024, initial_states=[init], resident=False)
+    a, b = LadderBatch(XYModel(), [(128, temps)], **kw), LadderBatch(XYModel(), [(128, temps)], **kw)
+    a.run(40, graph=False)
+    b.run(40, tune=True, graph=False)
+    a.check_errors()
+    np.testing.assert_array_equal(a.ladder_state(0), b.ladder_state(0))
+    for name in ("rng", "aux", "w2t", "t2w", "betas", "swap_counts", "trips", "e_run", "energies", "accepted",
+                 "clock"):
+        np.testing.assert_array_equal(getattr(a, name).copy_to_host(), getattr(b, name).copy_to_host(),
+                                      err_msg=name)
