@@ -1060,12 +1060,16 @@ class LadderBatch:
                 raise ValueError("sample_interval must be positive")
             self.allocate_samples(self.sweeps + si, si, n // si + 1)
 
+        per_group = []
+
         def tune_groups():
             total, trials = 0.0, []
+            per_group.clear()
             for g in self.groups:
                 res = self._tune_group(g, n, shapes, verbose)
                 total += res[0][0]
                 trials += res
+                per_group.append(res)
             return total, trials
 
         ragged = len(self._sizes()) > 1
@@ -1076,6 +1080,7 @@ class LadderBatch:
             self.split_by_size(True)
             many, many_trials = tune_groups()
             many_shapes = [(g.cluster_size, g.threads) for g in self.groups]
+            packed_shapes = self._side_by_side_shapes(per_group)
             # Trial windows launch every group once per window; a production
             # step replays graphs of resident launches, which hide most of
             # that cost.  So the grouping is chosen on a few real steps.
@@ -1085,6 +1090,18 @@ class LadderBatch:
             for g, (C, T) in zip(self.groups, many_shapes):
                 self._configure_group(g, C, T)
             side_run = self._time_steps(n)
+            side_shapes = many_shapes
+            if packed_shapes != many_shapes:
+                # Shapes chosen for sharing the GPU (below) rather than each
+                # group's fastest alone.
+                for g, (C, T) in zip(self.groups, packed_shapes):
+                    self._configure_group(g, C, T)
+                packed_run = self._time_steps(n)
+                if verbose:
+                    print(f"autotune: side by side {side_run:.3f} ms with each group's fastest shape, "
+                          f"{packed_run:.3f} ms with shapes {packed_shapes}")
+                if packed_run < side_run:
+                    side_run, side_shapes = packed_run, packed_shapes
             self.split_by_size(False)
             self.configure(*one_shape)
             one_run = self._time_steps(n)
@@ -1094,8 +1111,9 @@ class LadderBatch:
                       f"{side_run:.3f} ms side by side (steps)")
             best = min(many_run, side_run)
             if best < 0.98 * one_run:
-                self.split_by_size(True, concurrent=side_run < many_run)
-                for g, (C, T) in zip(self.groups, many_shapes):
+                side = side_run < many_run
+                self.split_by_size(True, concurrent=side)
+                for g, (C, T) in zip(self.groups, side_shapes if side else many_shapes):
                     self._configure_group(g, C, T)
                 self._graphs.clear()
                 self._resident_checked = False
@@ -1119,6 +1137,38 @@ class LadderBatch:
         self._resident_checked = False
         self.recompute_energy()
         return results
+
+    def _side_by_side_shapes(self, per_group):
+        """Shapes for the groups of a split batch running side by side, from
+        each group's trial times [(ms, C, T)]: a group whose launch holds the
+        fraction f of the GPU's co-resident clusters (its clusters over the
+        most that fit at once) for ms occupies f * ms of the GPU, and the
+        window takes at least the longest group and at least the groups'
+        summed occupancy; coordinate descent over the groups' shapes
+        minimises the larger of the two, starting from each group's fastest."""
+        opts = []
+        for g, res in zip(self.groups, per_group):
+            row = []
+            for ms, C, T in res:
+                m = self.max_clusters(C, T, g.idx)
+                if m < 1:
+                    continue
+                row.append((ms, min(1.0, min(m, len(g.idx)) / m) * ms, C, T))
+            opts.append(row)
+        pick = [0] * len(opts)
+
+        def cost(sel):
+            return max(max(opts[k][i][0] for k, i in enumerate(sel)), sum(opts[k][i][1] for k, i in enumerate(sel)))
+
+        for _ in range(8):
+            changed = False
+            for k in range(len(opts)):
+                best = min(range(len(opts[k])), key=lambda i: cost(pick[:k] + [i] + pick[k + 1:]))
+                if cost(pick[:k] + [best] + pick[k + 1:]) < cost(pick) - 1e-9:
+                    pick[k], changed = best, True
+            if not changed:
+                break
+        return [(opts[k][i][2], opts[k][i][3]) for k, i in enumerate(pick)]
 
     def _time_steps(self, n, windows=8):
         """ms per n-sweep window of `windows` windows run as production runs
