@@ -390,26 +390,25 @@ __global__ void kawamura_local_kernel(const float *__restrict__ state, int L,
     out[n + k] = kaw_local_energy(b, L, i, j, p[0], p[1], p[2], p[3], p[4], J);
 }
 
-__device__ __forceinline__ double kaw_bond64(const float *a, const float *n, double &weight, double &angle)
+// One bond of models/kawamura/measure.py:29-42 as float-float:
+// weight = (1 + tau tau_n) (d . d_n) and cos, sin of theta - theta_n (the
+// reference's float64 terms, to about 1e-14; GB300's float64 pipe issues at
+// a small fraction of the float32 rate).  Returns weight * cos.
+__device__ __forceinline__ ff kaw_bond_ff(const float *a, const float *n, ff &weight, ff &sin_term)
 {
-    const double dot = (double)a[2] * n[2] + (double)a[3] * n[3] + (double)a[4] * n[4];
-    weight = (1.0 + (double)a[1] * n[1]) * dot;
-    angle = (double)a[0] - (double)n[0];
-    return weight * cos(angle);
-}
-
-// The same bond with sin(angle) too, from one argument reduction.
-__device__ __forceinline__ double kaw_bond64_sc(const float *a, const float *n, double &weight, double &sin_angle)
-{
-    const double dot = (double)a[2] * n[2] + (double)a[3] * n[3] + (double)a[4] * n[4];
-    weight = (1.0 + (double)a[1] * n[1]) * dot;
-    double c;
-    sincos((double)a[0] - (double)n[0], &sin_angle, &c);
-    return weight * c;
+    const ff dot = ff_add(ff_add(ff_two_prod(a[2], n[2]), ff_two_prod(a[3], n[3])), ff_two_prod(a[4], n[4]));
+    weight = ff_mul(dot, ff_add_f(ff_two_prod(a[1], n[1]), 1.0f));
+    ff sn, cs;
+    ff_sincos(ff_diff(a[0], n[0]), &sn, &cs);
+    sin_term = ff_mul(weight, sn);
+    return ff_mul(weight, cs);
 }
 
 // models/kawamura/measure.py:14-122.  NC = 1 energy only; NC = 12 sums for
 // the 7 output channels (spin2 is formed from 6 tensor sums at the end).
+// Every per-site term is evaluated and accumulated per thread as
+// float-float on the float32 pipe (within about 1e-14 of the reference's
+// float64 terms); only the per-thread totals enter the float64 reduction.
 template <int NC>
 __global__ void kawamura_reduce_kernel(const float *__restrict__ state, int R, int L, float J,
                                        const int32_t *__restrict__ tidx,
@@ -419,37 +418,43 @@ __global__ void kawamura_reduce_kernel(const float *__restrict__ state, int R, i
     const ReplicaSpan sp = replica_span();
     const int r = sp.r;
     const float *b = state + (int64_t)r * L * L * 5;
-    double v[NC];
+    const ff third = ff_make(0x1.555556p-2f, -0x1.555556p-27f);  // 1/3
+    ff acc[NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) v[c] = 0.0;
+    for (int c = 0; c < NC; ++c) acc[c] = ff_make(0.0f, 0.0f);
     const bool need_e = cached == nullptr;
     for (int k = sp.first; k < L * L; k += sp.step) {
         const int i = k / L, j = k - i * L;
         const float *a = b + (int64_t)k * 5;
-        double w, ang, sin_x = 0.0;
-        const float *nx = b + ((int64_t)wrapi(i + 1, L) * L + j) * 5;
-        const double cx = NC == 12 ? kaw_bond64_sc(a, nx, w, sin_x) : kaw_bond64(a, nx, w, ang);
+        ff w, sin_x;
+        const ff cos_x = kaw_bond_ff(a, b + ((int64_t)wrapi(i + 1, L) * L + j) * 5, w, sin_x);
         if (need_e) {
-            double w2, ang2;
-            v[0] -= (double)J * (cx + kaw_bond64(a, b + ((int64_t)i * L + wrapi(j + 1, L)) * 5, w2, ang2));
+            ff w2, s2;
+            const ff cos_y = kaw_bond_ff(a, b + ((int64_t)i * L + wrapi(j + 1, L)) * 5, w2, s2);
+            acc[0] = ff_add(acc[0], ff_add(cos_x, cos_y));
         }
         if (NC == 12) {
-            const double th = a[0], dx = a[2], dy = a[3], dz = a[4];
-            double s2, c2;
-            sincos(2 * th, &s2, &c2);
-            v[NC == 12 ? 1 : 0] += a[1];
-            v[NC == 12 ? 2 : 0] += c2;
-            v[NC == 12 ? 3 : 0] += s2;
-            v[NC == 12 ? 4 : 0] += dx * dx - 1.0 / 3;
-            v[NC == 12 ? 5 : 0] += dy * dy - 1.0 / 3;
-            v[NC == 12 ? 6 : 0] += dz * dz - 1.0 / 3;
-            v[NC == 12 ? 7 : 0] += dx * dy;
-            v[NC == 12 ? 8 : 0] += dx * dz;
-            v[NC == 12 ? 9 : 0] += dy * dz;
-            v[NC == 12 ? 10 : 0] += cx;
-            v[NC == 12 ? 11 : 0] += w * sin_x;
+            constexpr int q = NC == 12 ? 1 : 0;  // channel offsets valid for NC == 12 only
+            const float dx = a[2], dy = a[3], dz = a[4];
+            ff s2t, c2t;
+            ff_sincos(ff_make(2.0f * a[0], 0.0f), &s2t, &c2t);  // 2 theta is exact
+            acc[q * 1] = ff_add_f(acc[q * 1], a[1]);
+            acc[q * 2] = ff_add(acc[q * 2], c2t);
+            acc[q * 3] = ff_add(acc[q * 3], s2t);
+            acc[q * 4] = ff_add(acc[q * 4], ff_add(ff_two_prod(dx, dx), ff_neg(third)));
+            acc[q * 5] = ff_add(acc[q * 5], ff_add(ff_two_prod(dy, dy), ff_neg(third)));
+            acc[q * 6] = ff_add(acc[q * 6], ff_add(ff_two_prod(dz, dz), ff_neg(third)));
+            acc[q * 7] = ff_add(acc[q * 7], ff_two_prod(dx, dy));
+            acc[q * 8] = ff_add(acc[q * 8], ff_two_prod(dx, dz));
+            acc[q * 9] = ff_add(acc[q * 9], ff_two_prod(dy, dz));
+            acc[q * 10] = ff_add(acc[q * 10], cos_x);
+            acc[q * 11] = ff_add(acc[q * 11], sin_x);
         }
     }
+    double v[NC];
+    v[0] = -(double)J * ff_to_double(acc[0]);
+#pragma unroll
+    for (int c = 1; c < NC; ++c) v[c] = ff_to_double(acc[c]);
     cluster_sum<NC>(v, scratch, part);
     if (sp.rank == 0 && threadIdx.x == 0) {
         const int d = tidx ? tidx[r] : r;
