@@ -98,6 +98,37 @@ __device__ __forceinline__ Site make_site(int p, int LP)
     return s;
 }
 
+// The plaquettes p, p + step, p + 2 step, ... of a strip with rows of LP:
+// (row, column) advanced by additions, without a division per visit.
+struct SiteWalk {
+    int pr, pc, dq, dr, LP;
+    __device__ __forceinline__ SiteWalk(int p, int step, int lp)
+        : pr(p / lp), pc(p - (p / lp) * lp), dq(step / lp), dr(step - (step / lp) * lp), LP(lp)
+    {
+    }
+    __device__ __forceinline__ void advance()
+    {
+        pc += dr;
+        pr += dq;
+        if (pc >= LP) {
+            pc -= LP;
+            ++pr;
+        }
+    }
+    __device__ __forceinline__ Site site() const
+    {
+        Site s;
+        s.pr = pr;
+        s.pc = pc;
+        s.o = (pr + 1) * LP;
+        s.om = s.o - LP;
+        s.op = s.o + LP;
+        s.pcm = pc == 0 ? LP - 1 : pc - 1;
+        s.pcp = pc + 1 == LP ? 0 : pc + 1;
+        return s;
+    }
+};
+
 // Neighbour accessor handed to the policies: every read is local.
 template <typename Cell>
 struct Nbrs {
@@ -448,14 +479,15 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
         // flight meanwhile.  Site p + T is touched only when it exists.
         ulonglong2 c0 = p < g.NPL ? rng_g[p] : zero;
         ulonglong2 c1 = p + T < g.NPL ? rng_g[p + T] : zero;
+        SiteWalk w0(p, 2 * T, g.LP), w1(p + T, 2 * T, g.LP);
 #pragma unroll 1
-        for (; p < g.NPL; p += 2 * T) {
+        for (; p < g.NPL; p += 2 * T, w0.advance(), w1.advance()) {
             const int q = p + T;
             const bool has1 = q < g.NPL;
             const ulonglong2 n0 = p + 2 * T < g.NPL ? rng_g[p + 2 * T] : zero;
             const ulonglong2 n1 = p + 3 * T < g.NPL ? rng_g[p + 3 * T] : zero;
-            const Site s0 = make_site(p, g.LP);
-            const Site s1 = make_site(has1 ? q : p, g.LP);
+            const Site s0 = w0.site();
+            const Site s1 = has1 ? w1.site() : s0;
             float *o0 = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
             float *o1 = own + (size_t)(C_ * g.NPL + (has1 ? q : p)) * M::kOwnFloats;
             typename M::Cell &me0 = cells[C_ * g.PS + s0.o + s0.pc];
@@ -487,11 +519,12 @@ __device__ __forceinline__ void global_rng_pass(const typename M::Args &a, const
     }
     ulonglong2 cur = p < g.NPL ? rng_g[p] : zero;
     ulonglong2 nx1 = p + T < g.NPL ? rng_g[p + T] : zero;
+    SiteWalk walk(p, T, g.LP);
 #pragma unroll 1
-    for (; p < g.NPL; p += T) {
+    for (; p < g.NPL; p += T, walk.advance()) {
         const ulonglong2 nx2 = p + 2 * T < g.NPL ? rng_g[p + 2 * T] : zero;
         ulonglong2 sv = cur;
-        const Site s = make_site(p, g.LP);
+        const Site s = walk.site();
         float *o = own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats;
         typename M::Cell &me = cells[C_ * g.PS + s.o + s.pc];
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
@@ -545,8 +578,9 @@ template <class M, int C_>
 __device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
                                                const StripCtx &g, FSum *v)
 {
-    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
-        const Site s = make_site(p, g.LP);
+    SiteWalk walk(threadIdx.x, blockDim.x, g.LP);
+    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x, walk.advance()) {
+        const Site s = walk.site();
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
         M::template measure<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
                                 own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, v);
@@ -557,8 +591,9 @@ template <class M, int C_>
 __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
                                               const StripCtx &g, FSum &e)
 {
-    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x) {
-        const Site s = make_site(p, g.LP);
+    SiteWalk walk(threadIdx.x, blockDim.x, g.LP);
+    for (int p = threadIdx.x; p < g.NPL; p += blockDim.x, walk.advance()) {
+        const Site s = walk.site();
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
         M::template energy_site<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
                                     own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, e);
