@@ -92,27 +92,13 @@ __device__ __forceinline__ float he3_gradient_difference(const float *state, int
     return delta_g;
 }
 
-__device__ __forceinline__ bool he3_color_site(int64_t t, int R, int L, int color, int &r, int &i, int &j)
-{
-    const int H = L >> 1;
-    const int64_t per = (int64_t)H * H;
-    if (t >= (int64_t)R * per) return false;
-    r = (int)(t / per);
-    const int rem = (int)(t - (int64_t)r * per);
-    const int row = rem / H, col = rem - row * H;
-    i = 2 * row + (color >> 1);
-    j = 2 * col + (color & 1);
-    return true;
-}
-
 // models/he3/update.py:178-227
 __global__ void he3_color_kernel(float *__restrict__ state, ulonglong2 *__restrict__ rng,
                                  const float *__restrict__ betas, int R, int L, int color, Coeff5 coeff,
                                  float K, float delta, float g_d)
 {
     int r, i, j;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!he3_color_site(t, R, L, color, r, i, j)) return;
+    if (!colour_grid_site(R, L, color, r, i, j)) return;
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
     ulonglong2 st = rng[idx];
     c32 psi[6];
@@ -156,8 +142,7 @@ __global__ void he3_gauss_color_kernel(float *__restrict__ state, ulonglong2 *__
                                        long long *__restrict__ counts)
 {
     int r, i, j;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!he3_color_site(t, R, L, color, r, i, j)) return;
+    if (!colour_grid_site(R, L, color, r, i, j)) return;
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
     const int64_t plane = (int64_t)R * L * L;
     const int ip = wrapi(i + 1, L), im = wrapi(i - 1, L), jp = wrapi(j + 1, L), jm = wrapi(j - 1, L);
@@ -316,6 +301,7 @@ __global__ void he3_local_diff_kernel(const float *__restrict__ state, int L, co
 inline int check_he3(const char *who, int R, int L, const float *coeff)
 {
     MCGB_REQUIRE(R >= 1, "%s: R must be >= 1", who);
+    MCGB_REQUIRE(R <= 32767, "%s: at most 32767 replicas (one grid layer per replica)", who);
     MCGB_REQUIRE(L >= 4 && L % 2 == 0, "%s: L must be even and >= 4", who);
     MCGB_REQUIRE(coeff != nullptr, "%s: null coefficients", who);
     return MCGB_OK;
@@ -340,8 +326,8 @@ extern "C" int mcgb_he3_update_color(float *state, void *rng, const float *betas
     if (int st = check_he3("he3_update_color", R, L, coefficients)) return st;
     MCGB_REQUIRE(state && rng && betas, "he3_update_color: null pointer");
     MCGB_REQUIRE(color >= 0 && color < 4, "he3_update_color: color must be 0..3");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
-    he3_color_kernel<<<blocks_for(n, 128), 128, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(R, L, 1, 128);
+    he3_color_kernel<<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         state, static_cast<ulonglong2 *>(rng), betas, R, L, color, make_coeff(coefficients), K, delta, g_d);
     return check_launch("he3_color_kernel");
 }
@@ -353,8 +339,8 @@ extern "C" int mcgb_he3_gaussian_update_color(float *state, void *rng, const flo
     if (int st = check_he3("he3_gaussian_update_color", R, L, coefficients)) return st;
     MCGB_REQUIRE(state && rng && betas && counts, "he3_gaussian_update_color: null pointer");
     MCGB_REQUIRE(color >= 0 && color < 4, "he3_gaussian_update_color: color must be 0..3");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
-    he3_gauss_color_kernel<<<blocks_for(n, 128), 128, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(R, L, 1, 128);
+    he3_gauss_color_kernel<<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         state, static_cast<ulonglong2 *>(rng), betas, R, L, color, make_coeff(coefficients), K, rho, mass, g_d,
         reinterpret_cast<long long *>(counts));
     return check_launch("he3_gauss_color_kernel");

@@ -16,36 +16,7 @@
 
 namespace mcgb {
 
-constexpr int kColorThreads = 256;
 constexpr int kReduceThreads = 256;
-
-// Maps a thread index to a visited site of colour `color`.
-__device__ __forceinline__ bool color_site(int64_t t, int R, int L, int color, int &r, int &i, int &j)
-{
-    const int H = L >> 1;
-    const int64_t per = (int64_t)H * H;
-    if (t >= (int64_t)R * per) return false;
-    r = (int)(t / per);
-    int rem = (int)(t - (int64_t)r * per);
-    int row = rem / H, col = rem - row * H;
-    i = 2 * row + (color >> 1);
-    j = 2 * col + (color & 1);
-    return true;
-}
-
-// Maps a thread to a site of colour `c0` or `c0 + 1` when `ncol` == 2
-// (colours 1 and 2 share no nearest-neighbour bond, so one launch does both).
-__device__ __forceinline__ bool phase_site(int64_t t, int R, int L, int c0, int ncol, int &r, int &i, int &j)
-{
-    const int H = L >> 1;
-    const int64_t per = (int64_t)R * H * H;
-    int extra = 0;
-    if (ncol == 2 && t >= per) {
-        t -= per;
-        extra = 1;
-    }
-    return color_site(t, R, L, c0 + extra, r, i, j);
-}
 
 inline unsigned grid_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
@@ -54,6 +25,7 @@ inline int check_lattice(const char *who, int R, int L)
     MCGB_REQUIRE(R >= 1, "%s: R must be >= 1", who);
     MCGB_REQUIRE(L >= 4 && L % 2 == 0, "%s: L must be even and >= 4", who);
     MCGB_REQUIRE((int64_t)R * L * L < (1ll << 40), "%s: lattice too large", who);
+    MCGB_REQUIRE(R <= 32767, "%s: at most 32767 replicas (one grid layer per replica and colour)", who);
     return MCGB_OK;
 }
 
@@ -65,8 +37,7 @@ __global__ void ising_phase_kernel(int8_t *__restrict__ spins, ulonglong2 *__res
                                    float J)
 {
     int r, i, j;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!phase_site(t, R, L, c0, ncol, r, i, j)) return;
+    if (!colour_grid_site(R, L, c0, r, i, j)) return;
     const int8_t *b = spins + (int64_t)r * L * L;
     const int s = b[i * L + j];
     const int up = b[wrapi(i - 1, L) * L + j];
@@ -135,8 +106,7 @@ __global__ void xy_color_kernel(float *__restrict__ theta, ulonglong2 *__restric
 {
     const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
     int r, i, j;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!phase_site(t, R, L, color, ncol, r, i, j)) return;
+    if (!colour_grid_site(R, L, color, r, i, j)) return;
     float *b = theta + (int64_t)r * L * L;
     const float th = b[i * L + j];
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
@@ -178,8 +148,7 @@ __global__ void xy64_color_kernel(double *__restrict__ theta, ulonglong2 *__rest
 {
     const double pi = 3.14159265358979323846, two_pi = 6.28318530717958647692;
     int rr, i, j;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!color_site(t, 1, L, color, rr, i, j)) return;
+    if (!colour_grid_site(1, L, color, rr, i, j)) return;
     double *b = theta + (int64_t)r * L * L;
     const double th = b[i * L + j];
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
@@ -328,8 +297,7 @@ __global__ void kawamura_color_kernel(float *__restrict__ state, ulonglong2 *__r
 {
     const float pi = 3.14159265358979323846f, two_pi = 6.28318530717958647692f;
     int r, i, j;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (!phase_site(t, R, L, color, ncol, r, i, j)) return;
+    if (!colour_grid_site(R, L, color, r, i, j)) return;
     const float *b = state + (int64_t)r * L * L * 5;
     float *site = state + (((int64_t)r * L + i) * L + j) * 5;
     const int64_t idx = (int64_t)r * L * L + (int64_t)i * L + j;
@@ -483,8 +451,8 @@ extern "C" int mcgb_ising_update_color(int8_t *spins, void *rng, const float *be
     if (int st = check_lattice("ising_update_color", R, L)) return st;
     MCGB_REQUIRE(spins && rng && betas, "ising_update_color: null pointer");
     MCGB_REQUIRE(color >= 0 && color < 4, "ising_update_color: color must be 0..3");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
-    ising_phase_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(R, L, 1);
+    ising_phase_kernel<<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         spins, static_cast<ulonglong2 *>(rng), betas, R, L, color, 1, J);
     return check_launch("ising_phase_kernel");
 }
@@ -495,14 +463,14 @@ extern "C" int mcgb_ising_sweep(int8_t *spins, void *rng, const float *betas, in
     if (int st = check_lattice("ising_sweep", R, L)) return st;
     MCGB_REQUIRE(spins && rng && betas, "ising_sweep: null pointer");
     MCGB_REQUIRE(n_sweeps >= 0, "ising_sweep: n_sweeps must be >= 0");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
+    const ColourGrid one = colour_grid(R, L, 1), two = colour_grid(R, L, 2);
     cudaStream_t s = as_stream(stream);
     for (int k = 0; k < n_sweeps; ++k) {
-        ising_phase_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, s>>>(
+        ising_phase_kernel<<<one.grid, one.block, 0, s>>>(
             spins, static_cast<ulonglong2 *>(rng), betas, R, L, 0, 1, J);
-        ising_phase_kernel<<<grid_for(2 * n, kColorThreads), kColorThreads, 0, s>>>(
+        ising_phase_kernel<<<two.grid, two.block, 0, s>>>(
             spins, static_cast<ulonglong2 *>(rng), betas, R, L, 1, 2, J);
-        ising_phase_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, s>>>(
+        ising_phase_kernel<<<one.grid, one.block, 0, s>>>(
             spins, static_cast<ulonglong2 *>(rng), betas, R, L, 3, 1, J);
     }
     return check_launch("ising_phase_kernel");
@@ -531,8 +499,8 @@ extern "C" int mcgb_xy_update_color(float *theta, void *rng, const float *betas,
     if (int st = check_lattice("xy_update_color", R, L)) return st;
     MCGB_REQUIRE(theta && rng && betas, "xy_update_color: null pointer");
     MCGB_REQUIRE(color >= 0 && color < 4, "xy_update_color: color must be 0..3");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
-    xy_color_kernel<false><<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(R, L, 1);
+    xy_color_kernel<false><<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         theta, static_cast<ulonglong2 *>(rng), betas, nullptr, R, L, color, 1, J, delta);
     return check_launch("xy_color_kernel");
 }
@@ -543,8 +511,8 @@ extern "C" int mcgb_xy_update_color_gauss(float *theta, void *rng, const float *
     if (int st = check_lattice("xy_update_color_gauss", R, L)) return st;
     MCGB_REQUIRE(theta && rng && betas && sigmas, "xy_update_color_gauss: null pointer");
     MCGB_REQUIRE(color >= 0 && color < 4, "xy_update_color_gauss: color must be 0..3");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
-    xy_color_kernel<true><<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(R, L, 1);
+    xy_color_kernel<true><<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         theta, static_cast<ulonglong2 *>(rng), betas, sigmas, R, L, color, 1, J, 0.0f);
     return check_launch("xy_color_kernel");
 }
@@ -555,17 +523,17 @@ extern "C" int mcgb_xy_sweep(float *theta, void *rng, const float *betas, const 
     if (int st = check_lattice("xy_sweep", R, L)) return st;
     MCGB_REQUIRE(theta && rng && betas, "xy_sweep: null pointer");
     MCGB_REQUIRE(n_sweeps >= 0, "xy_sweep: n_sweeps must be >= 0");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
     cudaStream_t s = as_stream(stream);
     ulonglong2 *st = static_cast<ulonglong2 *>(rng);
     for (int k = 0; k < n_sweeps; ++k) {
         for (int ph = 0; ph < 3; ++ph) {
             const int c0 = ph == 0 ? 0 : (ph == 1 ? 1 : 3), ncol = ph == 1 ? 2 : 1;
+            const ColourGrid cg = colour_grid(R, L, ncol);
             if (sigmas)
-                xy_color_kernel<true><<<grid_for(ncol * n, kColorThreads), kColorThreads, 0, s>>>(
+                xy_color_kernel<true><<<cg.grid, cg.block, 0, s>>>(
                     theta, st, betas, sigmas, R, L, c0, ncol, J, 0.0f);
             else
-                xy_color_kernel<false><<<grid_for(ncol * n, kColorThreads), kColorThreads, 0, s>>>(
+                xy_color_kernel<false><<<cg.grid, cg.block, 0, s>>>(
                     theta, st, betas, nullptr, R, L, c0, ncol, J, delta);
         }
     }
@@ -580,8 +548,8 @@ extern "C" int mcgb_xy64_update_color(double *theta, void *rng, const double *be
     MCGB_REQUIRE(theta && rng && betas, "xy64_update_color: null pointer");
     MCGB_REQUIRE(r >= 0 && r < R, "xy64_update_color: replica out of range");
     MCGB_REQUIRE(color >= 0 && color < 4, "xy64_update_color: color must be 0..3");
-    const int64_t n = (int64_t)(L / 2) * (L / 2);
-    xy64_color_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(1, L, 1);
+    xy64_color_kernel<<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         theta, static_cast<ulonglong2 *>(rng), betas, sigmas, w2t, L, r, color, J, delta);
     return check_launch("xy64_color_kernel");
 }
@@ -628,8 +596,8 @@ extern "C" int mcgb_kawamura_update_color(float *state, void *rng, const float *
     if (int st = check_lattice("kawamura_update_color", R, L)) return st;
     MCGB_REQUIRE(state && rng && betas, "kawamura_update_color: null pointer");
     MCGB_REQUIRE(color >= 0 && color < 4, "kawamura_update_color: color must be 0..3");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
-    kawamura_color_kernel<<<grid_for(n, kColorThreads), kColorThreads, 0, as_stream(stream)>>>(
+    const ColourGrid cg = colour_grid(R, L, 1);
+    kawamura_color_kernel<<<cg.grid, cg.block, 0, as_stream(stream)>>>(
         state, static_cast<ulonglong2 *>(rng), betas, R, L, color, 1, J, delta);
     return check_launch("kawamura_color_kernel");
 }
@@ -640,12 +608,12 @@ extern "C" int mcgb_kawamura_sweep(float *state, void *rng, const float *betas, 
     if (int st = check_lattice("kawamura_sweep", R, L)) return st;
     MCGB_REQUIRE(state && rng && betas, "kawamura_sweep: null pointer");
     MCGB_REQUIRE(n_sweeps >= 0, "kawamura_sweep: n_sweeps must be >= 0");
-    const int64_t n = (int64_t)R * (L / 2) * (L / 2);
     cudaStream_t s = as_stream(stream);
     for (int k = 0; k < n_sweeps; ++k) {
         for (int ph = 0; ph < 3; ++ph) {
             const int c0 = ph == 0 ? 0 : (ph == 1 ? 1 : 3), ncol = ph == 1 ? 2 : 1;
-            kawamura_color_kernel<<<grid_for(ncol * n, kColorThreads), kColorThreads, 0, s>>>(
+            const ColourGrid cg = colour_grid(R, L, ncol);
+            kawamura_color_kernel<<<cg.grid, cg.block, 0, s>>>(
                 state, static_cast<ulonglong2 *>(rng), betas, R, L, c0, ncol, J, delta);
         }
     }

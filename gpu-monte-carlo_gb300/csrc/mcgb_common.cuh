@@ -62,6 +62,43 @@ __device__ __forceinline__ float xoro_uniform_f32(ulonglong2 &s)
     return mcgb_unit_f32(xoro_next(s));
 }
 
+// ---------------------------------------------------------------- colour grids
+//
+// The per-colour kernels run one thread per site of a colour on a 3D grid
+// -- x over the L/2 columns, y over the L/2 rows of the colour's sublattice,
+// z over the replicas (and, for a launch of two colours, a second layer of
+// replicas for colour c0 + 1) -- the shape of the reference's
+// cuda.grid(3) launches, so a thread finds its site without divisions.
+struct ColourGrid {
+    dim3 grid, block;
+};
+
+inline ColourGrid colour_grid(int R, int L, int ncol, int threads = 256)
+{
+    const int H = L >> 1;
+    int bx = 32;
+    while (bx > 1 && bx / 2 >= H) bx /= 2;  // no wider than the rows (small lattices)
+    const int by = threads / bx;
+    ColourGrid g;
+    g.block = dim3((unsigned)bx, (unsigned)by, 1);
+    g.grid = dim3((unsigned)((H + bx - 1) / bx), (unsigned)((H + by - 1) / by), (unsigned)(R * ncol));
+    return g;
+}
+
+// Site (i, j) of replica r for this thread of a colour_grid(R, L, ncol)
+// launch of colour c0 (and c0 + 1 on the second layer); false outside.
+__device__ __forceinline__ bool colour_grid_site(int R, int L, int c0, int &r, int &i, int &j)
+{
+    const int H = L >> 1;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y * blockDim.y + threadIdx.y;
+    if (col >= H || row >= H) return false;
+    const int z = blockIdx.z, extra = z >= R ? 1 : 0;
+    r = z - extra * R;
+    i = 2 * row + ((c0 + extra) >> 1);
+    j = 2 * col + ((c0 + extra) & 1);
+    return true;
+}
+
 // ---------------------------------------------------------------- XY visit (reference arithmetic)
 //
 // models/xy/update.py:19-54 in two halves, shared by the per-colour kernel
