@@ -1019,9 +1019,10 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             }
         }
         if (!bulk)
-        for (int c = 0; c < 4; ++c)
-            for (int p = tid; p < g.NPL; p += T) {
-                const Site s = make_site(p, g.LP);
+        for (int c = 0; c < 4; ++c) {
+            SiteWalk walk(tid, T, g.LP);
+            for (int p = tid; p < g.NPL; p += T, walk.advance()) {
+                const Site s = walk.site();
                 Cell &me = cells[c * g.PS + s.o + s.pc];
                 M::load(a, strip_site<M>(rep, g, rank, base, gplane, c, p), me,
                         own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
@@ -1031,6 +1032,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 if (c >= 2 && s.pr == g.HP - 1)
                     *static_cast<Cell *>(__cluster_map_shared_rank(cells + c * g.PS + s.pc, g.dn)) = me;
             }
+        }
 
         // NPMAX > 0: the streams live in registers (the host launches this
         // variant only when every strip fits) or, for the shared-memory
@@ -1225,12 +1227,14 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                                static_cast<float2 *>(__cluster_map_shared_rank(parts, 0)) + rank * NP + NS);
         }
         if (win + 1 == n_windows) {
-        for (int c = 0; c < 4; ++c)
-            for (int p = tid; p < g.NPL; p += T) {
-                const Site s = make_site(p, g.LP);
+        for (int c = 0; c < 4; ++c) {
+            SiteWalk walk(tid, T, g.LP);
+            for (int p = tid; p < g.NPL; p += T, walk.advance()) {
+                const Site s = walk.site();
                 M::store(a, strip_site<M>(rep, g, rank, base, gplane, c, p), cells[c * g.PS + s.o + s.pc],
                          own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
             }
+        }
         if constexpr (SS) {
             for (int c = 0; c < 4; ++c)
                 for (int p = tid; p < g.NPL; p += T)
