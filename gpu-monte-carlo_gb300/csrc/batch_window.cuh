@@ -578,9 +578,12 @@ template <class M, int C_>
 __device__ __forceinline__ void measure_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
                                                const StripCtx &g, FSum *v)
 {
-    SiteWalk walk(threadIdx.x, blockDim.x, g.LP);
+    // Long loops (strips of more than two plaquettes per thread) step by
+    // additions; short ones divide once per plaquette, fewer in all.
+    const bool long_loop = g.NPL > 2 * (int)blockDim.x;
+    SiteWalk walk(long_loop ? threadIdx.x : 0, long_loop ? blockDim.x : 1, g.LP);
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x, walk.advance()) {
-        const Site s = walk.site();
+        const Site s = long_loop ? walk.site() : make_site(p, g.LP);
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
         M::template measure<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
                                 own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, v);
@@ -591,9 +594,10 @@ template <class M, int C_>
 __device__ __forceinline__ void energy_colour(const typename M::Ctx &ctx, typename M::Cell *cells, float *own,
                                               const StripCtx &g, FSum &e)
 {
-    SiteWalk walk(threadIdx.x, blockDim.x, g.LP);
+    const bool long_loop = g.NPL > 2 * (int)blockDim.x;
+    SiteWalk walk(long_loop ? threadIdx.x : 0, long_loop ? blockDim.x : 1, g.LP);
     for (int p = threadIdx.x; p < g.NPL; p += blockDim.x, walk.advance()) {
-        const Site s = walk.site();
+        const Site s = long_loop ? walk.site() : make_site(p, g.LP);
         const Nbrs<typename M::Cell> nb{cells, g.PS, s};
         M::template energy_site<C_>(ctx, nb, cells[C_ * g.PS + s.o + s.pc],
                                     own + (size_t)(C_ * g.NPL + p) * M::kOwnFloats, e);
@@ -1018,11 +1022,13 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                 load_strip_bulk<M, SS>(a, cells, own, sst, g, base, gplane, strip_bar, strip_phase, a.fx.error);
             }
         }
+        // Long loops step by additions (see measure_colour).
+        const bool long_loop = g.NPL > 2 * T;
         if (!bulk)
         for (int c = 0; c < 4; ++c) {
-            SiteWalk walk(tid, T, g.LP);
+            SiteWalk walk(long_loop ? tid : 0, long_loop ? T : 1, g.LP);
             for (int p = tid; p < g.NPL; p += T, walk.advance()) {
-                const Site s = walk.site();
+                const Site s = long_loop ? walk.site() : make_site(p, g.LP);
                 Cell &me = cells[c * g.PS + s.o + s.pc];
                 M::load(a, strip_site<M>(rep, g, rank, base, gplane, c, p), me,
                         own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
@@ -1228,9 +1234,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         }
         if (win + 1 == n_windows) {
         for (int c = 0; c < 4; ++c) {
-            SiteWalk walk(tid, T, g.LP);
+            SiteWalk walk(long_loop ? tid : 0, long_loop ? T : 1, g.LP);
             for (int p = tid; p < g.NPL; p += T, walk.advance()) {
-                const Site s = walk.site();
+                const Site s = long_loop ? walk.site() : make_site(p, g.LP);
                 M::store(a, strip_site<M>(rep, g, rank, base, gplane, c, p), cells[c * g.PS + s.o + s.pc],
                          own + (size_t)(c * g.NPL + p) * M::kOwnFloats);
             }
