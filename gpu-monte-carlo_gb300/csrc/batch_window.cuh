@@ -984,6 +984,17 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     }
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
     if (a.fx.enabled && tid == 0) *fxs = a.fx;
+    // The launch's sample schedule (sample_slot's, once per launch: the clock
+    // stands still within a launch): the first sweep after the clock due a
+    // sample and its ring slot; -1 without samples.
+    long long sched_next0 = -1;
+    int sched_slot0 = 0;
+    if (cm.samples != nullptr && cm.sample_interval > 0 && cm.n_slots > 0) {
+        const long long first = cm.first_sample_sweep, from = __ldcg(cm.clock) + 1;
+        const long long k = from <= first ? 0 : (from - first + cm.sample_interval - 1) / cm.sample_interval;
+        sched_next0 = first + k * cm.sample_interval;
+        sched_slot0 = (int)(k % cm.n_slots);
+    }
     if (M::kBulkLoad && tid == 0) mbar_init(strip_bar, 1);
     [[maybe_unused]] unsigned strip_phase = 0;
     // DSMEM stores below need every CTA of the cluster to be running.
@@ -1067,6 +1078,11 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         // only); values the exchange rewrites are re-read past L1 at each
         // window start.
         const int n_windows = a.fx.enabled && a.fx.n_windows > 1 ? a.fx.n_windows : 1;
+        // The sample schedule: the next sweep number due a sample and its
+        // ring slot, from the launch's schedule at the first window, then
+        // carried from window to window (the sweeps step them).
+        long long next_sample = sched_next0;
+        int next_slot = sched_slot0;
         for (int win = 0; win < n_windows; ++win) {
         const typename M::Ctx ctx = M::prepare(a, r, rep);
         const float e_hi0 = __ldcg(cm.e_run + 2 * r), e_lo0 = __ldcg(cm.e_run + 2 * r + 1);
@@ -1075,17 +1091,6 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         const long long sweep0 = __ldcg(cm.clock) + (long long)win * cm.n_sweeps;
         const int tslot = rep.ladder_start + __ldcg(cm.w2t + r);
         cluster_arrive();
-
-        // This window's sample schedule (sample_slot's, stepped without
-        // divisions): the next sweep number due a sample and its ring slot.
-        long long next_sample = -1;
-        int next_slot = 0;
-        if (cm.samples != nullptr && cm.sample_interval > 0 && cm.n_slots > 0) {
-            const long long first = cm.first_sample_sweep, from = sweep0 + 1;
-            const long long k = from <= first ? 0 : (from - first + cm.sample_interval - 1) / cm.sample_interval;
-            next_sample = first + k * cm.sample_interval;
-            next_slot = (int)(k % cm.n_slots);
-        }
 
         float dsum = 0.0f, dcomp = 0.0f;
         int nacc = 0;
