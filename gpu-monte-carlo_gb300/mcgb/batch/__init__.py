@@ -122,6 +122,30 @@ def lpt_work_lists(costs, n_clusters):
     return ptrs, idx, loads
 
 
+def side_by_side_pick(rows):
+    """Which option of each group to run when the groups of a window run side
+    by side.  rows[k] lists group k's options as (ms, occupancy, ...): its
+    time alone and the GPU time it takes (ms times the fraction of the GPU it
+    holds).  The window takes at least its longest group and at least the
+    summed occupancy; coordinate descent over the groups minimises the larger
+    of the two, starting from each group's first (fastest) option.  Returns
+    the chosen index per group."""
+    pick = [0] * len(rows)
+
+    def cost(sel):
+        return max(max(rows[k][i][0] for k, i in enumerate(sel)), sum(rows[k][i][1] for k, i in enumerate(sel)))
+
+    for _ in range(8):
+        changed = False
+        for k in range(len(rows)):
+            best = min(range(len(rows[k])), key=lambda i: cost(pick[:k] + [i] + pick[k + 1:]))
+            if cost(pick[:k] + [best] + pick[k + 1:]) < cost(pick) - 1e-9:
+                pick[k], changed = best, True
+        if not changed:
+            break
+    return pick
+
+
 def visit_costs(Ls, C, T):
     """Relative time a cluster of C CTAs x T threads spends on each replica of
     sizes Ls, for its work lists: the visits a thread makes per colour phase
@@ -1140,35 +1164,20 @@ class LadderBatch:
 
     def _side_by_side_shapes(self, per_group):
         """Shapes for the groups of a split batch running side by side, from
-        each group's trial times [(ms, C, T)]: a group whose launch holds the
-        fraction f of the GPU's co-resident clusters (its clusters over the
-        most that fit at once) for ms occupies f * ms of the GPU, and the
-        window takes at least the longest group and at least the groups'
-        summed occupancy; coordinate descent over the groups' shapes
-        minimises the larger of the two, starting from each group's fastest."""
-        opts = []
+        each group's trial times [(ms, C, T)] (side_by_side_pick); a group's
+        occupancy is its trial time scaled by the fraction of the GPU's
+        co-resident clusters its launch holds."""
+        rows = []
         for g, res in zip(self.groups, per_group):
             row = []
             for ms, C, T in res:
                 m = self.max_clusters(C, T, g.idx)
-                if m < 1:
-                    continue
-                row.append((ms, min(1.0, min(m, len(g.idx)) / m) * ms, C, T))
-            opts.append(row)
-        pick = [0] * len(opts)
-
-        def cost(sel):
-            return max(max(opts[k][i][0] for k, i in enumerate(sel)), sum(opts[k][i][1] for k, i in enumerate(sel)))
-
-        for _ in range(8):
-            changed = False
-            for k in range(len(opts)):
-                best = min(range(len(opts[k])), key=lambda i: cost(pick[:k] + [i] + pick[k + 1:]))
-                if cost(pick[:k] + [best] + pick[k + 1:]) < cost(pick) - 1e-9:
-                    pick[k], changed = best, True
-            if not changed:
-                break
-        return [(opts[k][i][2], opts[k][i][3]) for k, i in enumerate(pick)]
+                if m >= 1:
+                    row.append((ms, min(1.0, min(m, len(g.idx)) / m) * ms, C, T))
+            if not row:
+                return [(C, T) for _, C, T in (r[0] for r in per_group)]
+            rows.append(row)
+        return [(row[i][2], row[i][3]) for row, i in zip(rows, side_by_side_pick(rows))]
 
     def _time_steps(self, n, windows=8):
         """ms per n-sweep window of `windows` windows run as production runs
