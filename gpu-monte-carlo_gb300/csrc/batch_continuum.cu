@@ -71,11 +71,9 @@ struct KawamuraPolicy {
         float v1, v2, v3;  // acceptance uniforms of the three sub-moves
     };
 
-    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int, const mcgb_replica &, const Walker &wk)
     {
-        // betas and the map are rewritten by exchanges within a resident launch
-        return Ctx{__ldcg(a.c.betas + r), a.J, a.delta,
-                   kGauss ? __ldcg(a.sigma_t + rep.ladder_start + __ldcg(a.c.w2t + r)) : 0.0f};
+        return Ctx{wk.beta, a.J, a.delta, kGauss ? wk.sigma : 0.0f};
     }
     // A pair of standard normals from one draw (Box-Muller, fast intrinsics).
     static __device__ __forceinline__ float2 normal_pair(uint64_t bits)
@@ -464,10 +462,10 @@ struct He3Policy {
     using Ctx = He3Ctx;
     struct Prop {};
 
-    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &, const Walker &wk)
     {
         Ctx x;
-        x.beta = __ldcg(a.c.betas + r);  // rewritten by exchanges within a resident launch
+        x.beta = wk.beta;
         x.K = a.K;
         x.delta = a.delta;
         x.g_d = a.g_d;

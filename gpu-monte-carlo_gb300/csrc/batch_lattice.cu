@@ -55,11 +55,11 @@ struct IsingPolicy {
         unsigned long long m;  // x >> 11 of the visit's draw
     };
 
-    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int, const mcgb_replica &, const Walker &wk)
     {
         Ctx x;
         x.J = a.J;
-        const float beta = __ldcg(a.c.betas + r);  // rewritten by exchanges within a resident launch
+        const float beta = wk.beta;
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
             const float dE = (float)(4 * q - 8) * a.J;
@@ -157,14 +157,14 @@ struct XYPolicy {
         float tp, cp, sp, v;
     };
 
-    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &rep)
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int, const mcgb_replica &, const Walker &wk)
     {
         Ctx x;
-        x.beta = __ldcg(a.c.betas + r);  // rewritten by exchanges within a resident launch
+        x.beta = wk.beta;
         x.J = a.J;
         x.delta = a.delta;
         x.gauss = a.sigma_t != nullptr;
-        x.sigma = x.gauss ? __ldcg(a.sigma_t + rep.ladder_start + __ldcg(a.c.w2t + r)) : 0.0f;
+        x.sigma = x.gauss ? wk.sigma : 0.0f;
         return x;
     }
     // The (cos, sin) cache persists in `aux` between windows, so the chain
@@ -288,9 +288,9 @@ struct XYRefPolicy {
         float tp, v;
     };
 
-    static __device__ __forceinline__ Ctx prepare(const Args &a, int r, const mcgb_replica &)
+    static __device__ __forceinline__ Ctx prepare(const Args &a, int, const mcgb_replica &, const Walker &wk)
     {
-        return Ctx{__ldcg(a.c.betas + r), a.J, a.delta};
+        return Ctx{wk.beta, a.J, a.delta};
     }
     static __device__ __forceinline__ void load(const Args &a, int64_t site, Cell &cell, float *)
     {

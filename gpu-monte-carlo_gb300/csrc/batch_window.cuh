@@ -42,7 +42,8 @@
 // per-site shared-memory record neighbours read), kOwnFloats (extra
 // per-site floats only the owner reads), kChannels, kSplitMiddle, Prop (the
 // per-visit proposal), and
-//   Ctx  prepare(const Args&, int r, const mcgb_replica&)
+//   Ctx  prepare(const Args&, int r, const mcgb_replica&, const Walker&)  (the walker's
+//        beta, proposal width and slot for the window)
 //   void load(const Args&, int64_t site, Cell&, float* own)
 //   void store(const Args&, int64_t site, const Cell&, const float* own)
 //   Prop propose<c>(const Ctx&, const Cell&, const float* own, ulonglong2&)
@@ -190,13 +191,48 @@ constexpr size_t kFusedCopyBytes = (sizeof(FusedExchange) + 15) & ~static_cast<s
 // The mbarrier the bulk strip loads complete on (8 bytes, padded to 16).
 constexpr size_t kStripBarBytes = 16;
 
+// The walker a window runs: its beta, its proposal width (sigma_t of its
+// slot with per-temperature widths, else 0) and its slot in the ladder.
+struct Walker {
+    float beta, sigma;
+    int slot;
+};
+
+// What a resident launch carries in each CTA from one window of a replica to
+// the next, so that no window starts or ends on a global load: the walker
+// after the exchange (written into every CTA of the cluster by rank 0
+// before the cluster barrier that ends the window; at a replica's first
+// window each CTA's own copy of the walker it loaded), rank 0's running
+// energy and acceptance count, and the launch's clock {sweeps, rounds},
+// which stands still within a launch.
+struct WindowCarry {
+    Walker next;
+    float e_hi, e_lo;
+    long long accepted;
+    long long clock0, rounds0;
+};
+constexpr size_t kCarryBytes = (sizeof(WindowCarry) + 15) & ~static_cast<size_t>(15);
+// A launch's sample schedule with no sample due within the launch.
+constexpr int kNoSample = 0x3fffffff;
+
+// The walker of replica r as the device tables hold it.
+template <class Args>
+__device__ __forceinline__ Walker load_walker(const Args &a, int r, const mcgb_replica &rep)
+{
+    Walker w;
+    w.beta = __ldcg(a.c.betas + r);
+    w.slot = __ldcg(a.c.w2t + r);
+    w.sigma = a.sigma_t != nullptr ? __ldcg(a.sigma_t + rep.ladder_start + w.slot) : 0.0f;
+    return w;
+}
+
 // Shared memory of a strip with npl plaquettes in rows of lp (with
 // `streams`, also the strip's four colours of RNG streams, 16 B a site).
 template <class M>
 __host__ __device__ inline size_t window_smem_bytes(long long npl, long long lp, bool streams = false)
 {
     return sizeof(double) * (kRedDoubles + 32 * (M::kSums + 3) + kMaxCluster * part_slots<M>()) + kFusedCopyBytes +
-           kStripBarBytes +
+           kStripBarBytes + kCarryBytes +
            (size_t)4 * (npl + 2 * lp) * sizeof(typename M::Cell) + 16 +
            (size_t)4 * npl * sizeof(float) * M::kOwnFloats + (streams ? (size_t)4 * npl * 16 + 16 : 0);
 }
@@ -782,10 +818,14 @@ __device__ __forceinline__ bool exchange_accepts(double u, double log_ratio)
 // settling them at the new slot is then stores.  Decisions, maps, counters,
 // round trips and sample slots are exchange_ladder's on the same window.
 // Called by the 32 threads of warp 0; kept light in registers, because the
-// window kernel keeps its sweep state live across the call.
-static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int start, int R, int ladder, int r,
-                                                  int s, float b, double e, long long sweep, long long rounds,
-                                                  int slot, bool wait)
+// window kernel keeps its sweep state live across the call.  Returns, on
+// every lane, the walker for the next window when `wait` (its slot, its
+// beta: its own, the partner's known to the decider, or re-read by a waiter
+// whose pair swapped; and the proposal width of the slot, from `sigma_t`
+// when not null, both candidates loaded ahead of the decision).
+static __device__ __noinline__ Walker pair_finished(const FusedExchange &fx, const float *sigma_t, int start, int R,
+                                                    int ladder, int r, int s, float b, double e, long long sweep,
+                                                    long long rounds, int slot, bool wait)
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -821,6 +861,11 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
     // round, which this walker's own rounds have ordered before this load.
     ulonglong2 st = make_ulonglong2(0, 0);
     if (lane == 2 && left >= 0) st = __ldcg(x.rng + poff + left);
+    // The proposal widths of the walker's slot (lane 4) and its partner's
+    // (lane 5): sigma_t does not change within a launch.
+    float sg = 0.0f;
+    if (sigma_t != nullptr && (lane == 4 || (lane == 5 && left >= 0)))
+        sg = __ldcg(sigma_t + start + (lane == 4 ? s : partner));
     // Lane 0 posts; the stream travels to it while the atomic is in flight.
     unsigned long long got_lo = 0, got_hi = 0;
     if (lane == 0 && left >= 0)
@@ -829,8 +874,10 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
     st.x = __shfl_sync(full, st.x, 2);
     st.y = __shfl_sync(full, st.y, 2);
 
-    // walker w ends at slot t0 (-1: unknown); walker w1 (-1: none) at t1
+    // walker w ends at slot t0 (-1: unknown) with beta nb; walker w1 (-1:
+    // none) at t1
     int t0 = -1, w1 = -1, t1 = -1;
+    float nb = b;
     if (lane == 0) {
         if (left < 0) {
             t0 = s;  // no partner this round
@@ -869,6 +916,7 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
             *box = make_double2(0.0, 0.0);
             store_release(fx.decided + start + left, tag << 1 | swapped);
             t0 = swapped ? partner : s;
+            if (swapped) nb = bq;
             if (!wait) {
                 w1 = wq;
                 t1 = swapped ? s : partner;
@@ -883,6 +931,8 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
                 const int v = load_acquire(fx.decided + start + left);
                 if ((v >> 1) == tag) {
                     t0 = (v & 1) ? partner : s;
+                    // The decider wrote the swapped betas before its release.
+                    if (v & 1) nb = __ldcg(x.betas + r);
                     break;
                 }
                 __nanosleep(ns);
@@ -893,6 +943,11 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
     t0 = __shfl_sync(full, t0, 0);
     w1 = __shfl_sync(full, w1, 0);
     t1 = __shfl_sync(full, t1, 0);
+    Walker next;
+    next.slot = t0;
+    next.beta = __shfl_sync(full, nb, 0);
+    const float sg_own = __shfl_sync(full, sg, 4), sg_partner = __shfl_sync(full, sg, 5);
+    next.sigma = t0 == s ? sg_own : sg_partner;
     __syncwarp();  // orders lane 0's acquire before the other lanes' reads
 
     // Settle: round-trip counters (lane 1 for this walker, lane 3 for the
@@ -921,11 +976,12 @@ static __device__ __noinline__ void pair_finished(const FusedExchange &fx, int s
             }
         }
     }
-    if (slot < 0) return;
+    if (slot < 0) return next;
     double *out = x.samples + (size_t)slot * x.channels * x.n_temps_total + start;
     if (t0 >= 0 && lane < x.channels) out[(size_t)lane * x.n_temps_total + t0] = own;
     if (t1 >= 0 && lane < x.channels)
         out[(size_t)lane * x.n_temps_total + t1] = __ldcg(x.staging + (size_t)lane * n + start + w1);
+    return next;
 }
 
 // The global-stream variant with two visits in flight (policies with
@@ -969,7 +1025,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     float2 *parts = reinterpret_cast<float2 *>(scratch + 32 * (NS + 3));  // [kMaxCluster][NP], rank 0's used
     FusedExchange *fxs = reinterpret_cast<FusedExchange *>(parts + kMaxCluster * NP);
     uint64_t *strip_bar = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(fxs) + kFusedCopyBytes);
-    Cell *cells = reinterpret_cast<Cell *>(reinterpret_cast<unsigned char *>(strip_bar) + kStripBarBytes);
+    WindowCarry *carry =
+        reinterpret_cast<WindowCarry *>(reinterpret_cast<unsigned char *>(strip_bar) + kStripBarBytes);
+    Cell *cells = reinterpret_cast<Cell *>(reinterpret_cast<unsigned char *>(carry) + kCarryBytes);
 
     const WindowCommon &cm = a.c;
     // The work lists hold n_clusters entries for clusters of cluster_size
@@ -984,18 +1042,27 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
     }
     ulonglong2 *rng_g = static_cast<ulonglong2 *>(cm.rng);
     if (a.fx.enabled && tid == 0) *fxs = a.fx;
+    // A resident launch runs n_windows windows with the strip on chip,
+    // exchanging between them (each walker waits for its pair's decision
+    // only).
+    const int n_windows = a.fx.enabled && a.fx.n_windows > 1 ? a.fx.n_windows : 1;
     // The launch's sample schedule (sample_slot's, once per launch: the clock
-    // stands still within a launch): the first sweep after the clock due a
-    // sample and its ring slot; -1 without samples.
-    long long sched_next0 = -1;
-    int sched_slot0 = 0;
+    // stands still within a launch): the sweeps from the launch's start to
+    // the first one due a sample (kNoSample: none within the launch), and
+    // that sample's ring slot.
+    int sched_due0 = kNoSample, sched_slot0 = 0;
     if (cm.samples != nullptr && cm.sample_interval > 0 && cm.n_slots > 0) {
-        const long long first = cm.first_sample_sweep, from = __ldcg(cm.clock) + 1;
+        const long long clock0 = __ldcg(cm.clock), first = cm.first_sample_sweep, from = clock0 + 1;
         const long long k = from <= first ? 0 : (from - first + cm.sample_interval - 1) / cm.sample_interval;
-        sched_next0 = first + k * cm.sample_interval;
+        const long long due = first + k * cm.sample_interval - clock0;
+        if (due <= (long long)n_windows * cm.n_sweeps) sched_due0 = (int)due;
         sched_slot0 = (int)(k % cm.n_slots);
     }
     if (M::kBulkLoad && tid == 0) mbar_init(strip_bar, 1);
+    if (tid == 0) {
+        carry->clock0 = __ldcg(cm.clock);
+        carry->rounds0 = __ldcg(cm.clock + 1);
+    }
     [[maybe_unused]] unsigned strip_phase = 0;
     // DSMEM stores below need every CTA of the cluster to be running.
     cluster.sync();
@@ -1073,23 +1140,32 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
                     for (int p = tid; p < g.NPL; p += T)
                         sst[c * g.NPL + p] = rng_g[strip_site<M>(rep, g, rank, base, gplane, c, p)];
         }
-        // A resident launch runs n_windows windows with the strip on chip,
-        // exchanging between them (each walker waits for its pair's decision
-        // only); values the exchange rewrites are re-read past L1 at each
-        // window start.
-        const int n_windows = a.fx.enabled && a.fx.n_windows > 1 ? a.fx.n_windows : 1;
-        // The sample schedule: the next sweep number due a sample and its
-        // ring slot, from the launch's schedule at the first window, then
-        // carried from window to window (the sweeps step them).
-        long long next_sample = sched_next0;
-        int next_slot = sched_slot0;
+        // The sample schedule: the sweeps from the window's start to the next
+        // one due a sample (sweep s of the window is due when s + 1 == due)
+        // and its ring slot, from the launch's schedule at the first window,
+        // then carried from window to window.
+        int due = sched_due0, next_slot = sched_slot0;
         for (int win = 0; win < n_windows; ++win) {
-        const typename M::Ctx ctx = M::prepare(a, r, rep);
-        const float e_hi0 = __ldcg(cm.e_run + 2 * r), e_lo0 = __ldcg(cm.e_run + 2 * r + 1);
-        // A fused launch advances the clock once, at its end, after every
-        // cluster has finished its windows: within it the clock stands still.
-        const long long sweep0 = __ldcg(cm.clock) + (long long)win * cm.n_sweeps;
-        const int tslot = rep.ladder_start + __ldcg(cm.w2t + r);
+        // The walker and the running energy: from the device tables at a
+        // replica's first window, then as the previous window's exchange
+        // left them (carried on chip, published by the barrier that ended
+        // that window).
+        // Rank 0 reads the running energy and the walker's slot from its
+        // carry where it needs them (in no register across the sweeps).
+        Walker wk;
+        if (win == 0) {
+            wk = load_walker(a, r, rep);
+            if (tid == 0) {
+                carry->next = wk;
+                if (rank == 0) {
+                    carry->e_hi = __ldcg(cm.e_run + 2 * r);
+                    carry->e_lo = __ldcg(cm.e_run + 2 * r + 1);
+                }
+            }
+        } else {
+            wk = carry->next;
+        }
+        const typename M::Ctx ctx = M::prepare(a, r, rep, wk);
         cluster_arrive();
 
         float dsum = 0.0f, dcomp = 0.0f;
@@ -1100,7 +1176,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
 #define MCGB_COMBINE_PENDING()                                                                              \
     if (pend != -1) {                                                                                       \
         if (rank == 0 && tid < 32)                                                                          \
-            combine_sample<M>(ctx, cm, parts, red, C, pend, r, tslot, e_hi0, e_lo0, a.n_replicas);          \
+            combine_sample<M>(ctx, cm, parts, red, C, pend, r, rep.ladder_start + carry->next.slot,        \
+                              carry->e_hi, carry->e_lo, a.n_replicas);                                      \
         pend = -1;                                                                                          \
     }
         [[maybe_unused]] typename M::Prop pa[NK], pb[NK];
@@ -1121,7 +1198,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             // (an exchange may change the temperature before the next one)
             // nor after a sampled sweep (the sample reads the state between
             // the two).
-            const bool sample_due = sweep0 + s + 1 == next_sample;
+            const bool sample_due = s + 1 == due;
             [[maybe_unused]] const bool merge =
                 !M::kSplitMiddle && (M::kPipeline || !regs) && s + 1 < cm.n_sweeps && !sample_due;
             if constexpr (!M::kPipeline && regs) {
@@ -1193,9 +1270,9 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             c0_done = merge;
 
             comp_add(dsum, dcomp, dacc);
-            if (sweep0 + s + 1 == next_sample) {
+            if (sample_due) {
                 const int slot = next_slot;
-                next_sample += cm.sample_interval;
+                due += cm.sample_interval;
                 next_slot = next_slot + 1 == cm.n_slots ? 0 : next_slot + 1;
                 // Measure the strip before arriving at the barrier that ends
                 // the sweep.  Once this CTA's own colour-3 moves are done (a
@@ -1219,11 +1296,12 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         cluster_wait();
         MCGB_COMBINE_PENDING()
 #undef MCGB_COMBINE_PENDING
-        // Loaded ahead of the epilogue: the acceptance count, and for the
-        // exchange the walker's beta and the exchange rounds before this one.
-        const long long acc_prev = rank == 0 && tid == 0 ? __ldcg(cm.accepted + r) : 0;
-        const float beta_now = a.fx.enabled && rank == 0 && tid == 0 ? __ldcg(cm.betas + r) : 0.0f;
-        const long long rounds = a.fx.enabled && rank == 0 && tid < 32 ? __ldcg(cm.clock + 1) + win : 0;
+        // The acceptance count, and for the exchange the walker's beta and
+        // the exchange rounds before this one.
+        const long long acc_prev =
+            rank == 0 && tid == 0 ? (win == 0 ? __ldcg(cm.accepted + r) : carry->accepted) : 0;
+        const float beta_now = a.fx.enabled && rank == 0 && tid == 0 ? carry->next.beta : 0.0f;
+        const long long rounds = a.fx.enabled && rank == 0 && tid < 32 ? carry->rounds0 + win : 0;
         double e_now = 0.0;
         float e_hi = 0.0f, e_lo = 0.0f;
         long long acc_now = 0;
@@ -1282,8 +1360,8 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             } else {
                 // Compensated (hi, lo) float update of the running energy.
                 float s1, e1;
-                two_sum(e_hi0, de.hi, s1, e1);
-                const float lo = e_lo0 + e1 + de.lo;
+                two_sum(carry->e_hi, de.hi, s1, e1);
+                const float lo = carry->e_lo + e1 + de.lo;
                 two_sum(s1, lo, hi, lo2);
                 e_now = (double)hi + (double)lo2;
             }
@@ -1292,15 +1370,25 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
             acc_now = acc_prev + (long long)na.value();
         }
         __syncwarp();
+        Walker nw{};
         if (a.fx.enabled && rank == 0 && tid < 32)
-            pair_finished(*fxs, rep.ladder_start, rep.n_temps, rep.ladder, r, tslot - rep.ladder_start, beta_now,
-                          e_now, sweep0 + cm.n_sweeps, rounds, end_slot, win + 1 < n_windows);
+            nw = pair_finished(*fxs, a.sigma_t, rep.ladder_start, rep.n_temps, rep.ladder, r,
+                               carry->next.slot, beta_now, e_now, carry->clock0 + (long long)(win + 1) * cm.n_sweeps,
+                               rounds, end_slot,
+                               win + 1 < n_windows);
+        // The next window's walker into every CTA of the cluster (lane k,
+        // rank k), published by the cluster barrier below.
+        if (win + 1 < n_windows && rank == 0 && tid < C)
+            *static_cast<Walker *>(__cluster_map_shared_rank(&carry->next, tid)) = nw;
         // After the exchange, whose releasing atomic need not wait for them.
         if (rank == 0 && tid == 0) {
             cm.energies[r] = e_now;
             cm.e_run[2 * r] = e_hi;
             cm.e_run[2 * r + 1] = e_lo;
             cm.accepted[r] = acc_now;
+            carry->e_hi = e_hi;
+            carry->e_lo = e_lo;
+            carry->accepted = acc_now;
         }
         __syncwarp();  // the aligned cluster barriers need warp 0 converged again
         // Between windows of a resident launch every CTA waits for the new
@@ -1311,6 +1399,7 @@ __global__ void __launch_bounds__(window_max_threads<M, NPMAX>(), 1) window_kern
         // replica of the same size pushes only into halo rows, which the
         // write-back does not read; one of another size waited above.
         if (win + 1 < n_windows) cluster.sync();
+        if (due != kNoSample) due -= cm.n_sweeps;
         }  // windows
     }
     if (a.fx.enabled && rank == 0 && tid == 0) launch_finished(a.fx, cm, (int)(gridDim.x / C));
