@@ -1126,6 +1126,7 @@ class LadderBatch:
                           f"{packed_run:.3f} ms with shapes {packed_shapes}")
                 if packed_run < side_run:
                     side_run, side_shapes = packed_run, packed_shapes
+            side_shapes, side_run = self._refine_side_by_side(per_group, side_shapes, side_run, n, verbose)
             self.split_by_size(False)
             self.configure(*one_shape)
             one_run = self._time_steps(n)
@@ -1161,6 +1162,51 @@ class LadderBatch:
         self._resident_checked = False
         self.recompute_energy()
         return results
+
+    def _refine_side_by_side(self, per_group, shapes, best_ms, n, verbose=False, tolerance=0.3, budget=10,
+                             margin=0.03):
+        """Side-by-side groups on real steps: a group's shapes whose time
+        alone is within `tolerance` of its fastest can share the GPU with the
+        other groups' launches better or worse than those times say (a
+        group of many small CTAs beside one of few large ones), so each such
+        runner-up is timed in place of the group's current shape, the slowest
+        groups first, at most `budget` timings.  A runner-up replaces the
+        current shape only when it is faster by `margin` twice: in its own
+        timing and again when both are timed once more (the minimum over
+        several noisy timings would otherwise favour noise); the time of the
+        shapes it came with stands otherwise.  The kept shapes are
+        configured.  Returns (shapes, ms per window)."""
+        shapes = list(shapes)
+        order = sorted(range(len(per_group)), key=lambda k: -per_group[k][0][0])
+        tried = 0
+
+        def timed(sh):
+            nonlocal tried
+            for g, (c, t) in zip(self.groups, sh):
+                self._configure_group(g, c, t)
+            tried += 1
+            return self._time_steps(n)
+
+        for k in order:
+            fastest = per_group[k][0][0]
+            for ms, C, T in per_group[k]:
+                if tried >= budget:
+                    break
+                if (C, T) == shapes[k] or ms > (1.0 + tolerance) * fastest:
+                    continue
+                trial = shapes[:k] + [(C, T)] + shapes[k + 1:]
+                run = timed(trial)
+                if verbose:
+                    print(f"autotune: side by side with {trial}: {run:.3f} ms against {best_ms:.3f} ms")
+                if run < (1.0 - margin) * best_ms:
+                    current, again = timed(shapes), timed(trial)
+                    if verbose:
+                        print(f"autotune: again {again:.3f} ms against {current:.3f} ms")
+                    if again < (1.0 - margin) * current:
+                        best_ms, shapes = again, trial
+        for g, (c, t) in zip(self.groups, shapes):
+            self._configure_group(g, c, t)
+        return shapes, best_ms
 
     def _side_by_side_shapes(self, per_group):
         """Shapes for the groups of a split batch running side by side, from
