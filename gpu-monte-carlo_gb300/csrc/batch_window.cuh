@@ -943,11 +943,14 @@ static __device__ __noinline__ Walker pair_finished(const FusedExchange &fx, con
     t0 = __shfl_sync(full, t0, 0);
     w1 = __shfl_sync(full, w1, 0);
     t1 = __shfl_sync(full, t1, 0);
+    // A waiter that gave up (error flag raised, t0 = -1) keeps its slot and
+    // beta for the next window, so no index below ever goes out of the
+    // ladder.
     Walker next;
-    next.slot = t0;
+    next.slot = t0 >= 0 ? t0 : s;
     next.beta = __shfl_sync(full, nb, 0);
     const float sg_own = __shfl_sync(full, sg, 4), sg_partner = __shfl_sync(full, sg, 5);
-    next.sigma = t0 == s ? sg_own : sg_partner;
+    next.sigma = next.slot == s ? sg_own : sg_partner;
     __syncwarp();  // orders lane 0's acquire before the other lanes' reads
 
     // Settle: round-trip counters (lane 1 for this walker, lane 3 for the
