@@ -459,9 +459,11 @@ int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, const mcgb_ba
                             int32_t *sync, int n_windows, void *stream);
 /* No counterpart in the reference.  Polls of a resident launch's wait
  * between windows before it gives up and raises the error flag (default
- * 2^22, about a second; negative restores the default).  Applies to later
- * calls; returns the previous value.  With 0 every such wait gives up before
- * its first poll, which is how the timeout path is tested. */
+ * 2^22, about a second; negative restores the default); a walker whose wait
+ * gave up runs the launch's later windows at the slot and beta it had.
+ * Applies to later calls; returns the previous value.  With 0 every such
+ * wait gives up before its first poll, which is how the timeout path is
+ * tested. */
 int64_t mcgb_batch_set_wait_limit(int64_t polls);
 /* Advance the device clock: clock[0] += n_sweeps, clock[1] += exchanged, so
  * a captured graph of windows and exchanges can be replayed. */
