@@ -110,8 +110,10 @@ inline int validate_window(const mcgb_batch_window &w)
     MCGB_REQUIRE(w.cluster_size >= 1 && w.cluster_size <= 16, "batch window: cluster_size must be 1..16");
     MCGB_REQUIRE(w.threads >= 32 && w.threads <= 1024 && w.threads % 32 == 0,
                  "batch window: threads must be a multiple of 32 in [32, 1024]");
-    MCGB_REQUIRE(w.n_sweeps >= 0, "batch window: n_sweeps must be >= 0");
-    MCGB_REQUIRE(w.samples == nullptr || (w.n_slots >= 1 && w.n_temps_total >= 1 && w.sample_interval >= 1),
+    MCGB_REQUIRE(w.n_sweeps >= 0 && w.n_sweeps <= kMaxWindowSweeps, "batch window: n_sweeps must be in [0, %d]",
+                 kMaxWindowSweeps);
+    MCGB_REQUIRE(w.samples == nullptr || (w.n_slots >= 1 && w.n_temps_total >= 1 && w.sample_interval >= 1 &&
+                                          w.sample_interval <= kMaxWindowSweeps),
                  "batch window: bad sample buffer");
     for (int r = 0; r < w.n_replicas; ++r) {
         const mcgb_replica &rep = w.host_table[r];

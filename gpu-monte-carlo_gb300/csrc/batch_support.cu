@@ -194,6 +194,8 @@ extern "C" int mcgb_batch_run_resident(int model, const mcgb_batch_window *w, co
     MCGB_REQUIRE(w && pt, "run_resident: null argument block");
     MCGB_REQUIRE(sync != nullptr, "run_resident: null sync counters");
     MCGB_REQUIRE(n_windows >= 1, "run_resident: n_windows must be >= 1");
+    MCGB_REQUIRE((long long)n_windows * w->n_sweeps <= kMaxLaunchSweeps,
+                 "run_resident: at most %lld sweeps a launch", kMaxLaunchSweeps);
     MCGB_REQUIRE(n_windows == 1 || w->n_clusters == work_count(*w),
                  "run_resident: a resident launch needs one cluster per replica it runs");
     if (int st = check_exchange(*w, *pt)) return st;

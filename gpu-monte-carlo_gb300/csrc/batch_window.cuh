@@ -214,6 +214,12 @@ struct WindowCarry {
 constexpr size_t kCarryBytes = (sizeof(WindowCarry) + 15) & ~static_cast<size_t>(15);
 // A launch's sample schedule with no sample due within the launch.
 constexpr int kNoSample = 0x3fffffff;
+// Sweeps a window may run, and sweeps a launch may run in all (the host
+// refuses more), so that the schedule's int countdown -- at most a launch's
+// sweeps plus one sample interval -- stays below kNoSample.
+constexpr int kMaxWindowSweeps = 1 << 24;
+constexpr long long kMaxLaunchSweeps = 1ll << 28;
+static_assert(kMaxLaunchSweeps + kMaxWindowSweeps < kNoSample, "sample countdown range");
 
 // The walker of replica r as the device tables hold it.
 template <class Args>

@@ -27,6 +27,9 @@ MODEL_ISING_REF, MODEL_XY_REF = 6, 7
 # per CTA: one per thread of a 1024-thread CTA (the shared-memory stream
 # variant).
 MAX_PLAQUETTES = 1024
+# Sweeps of one window launch (the library takes up to 2^24); longer runs
+# take several launches, which continue the chain bit for bit.
+MAX_LAUNCH_SWEEPS = 1 << 20
 
 
 def _shape(L):
@@ -99,7 +102,15 @@ class WindowSweeps:
         return cls(runtime, model_id, C, T, min(runtime.R, n.value))
 
     def enqueue(self, n_sweeps):
-        """n_sweeps sweeps of every replica, one launch on the current stream."""
+        """n_sweeps sweeps of every replica on the current stream: one launch,
+        or one per MAX_LAUNCH_SWEEPS sweeps of a longer run."""
+        n_sweeps = int(n_sweeps)
+        while n_sweeps > 0:
+            n = min(n_sweeps, MAX_LAUNCH_SWEEPS)
+            self._launch(n)
+            n_sweeps -= n
+
+    def _launch(self, n_sweeps):
         rt = self.runtime
         w = BatchWindow()
         w.table, w.host_table, w.n_replicas = self.table.ptr, self.table_host.ctypes.data, rt.R

@@ -346,8 +346,9 @@ typedef struct mcgb_batch_window {
     int32_t n_temps_total, n_slots;
     const int64_t *clock;           /* device {sweeps completed, exchange rounds} before the window */
     int64_t first_sample_sweep;     /* cumulative sweep number of sample slot 0 */
-    int32_t sample_interval;        /* 0 = no samples */
-    int32_t n_sweeps;               /* sweeps in this window */
+    int32_t sample_interval;        /* 0 = no samples; at most 2^24 */
+    int32_t n_sweeps;               /* sweeps in this window, 0 .. 2^24 (a resident launch: at
+                                       most 2^28 over its windows) */
     float J, delta;                 /* Ising/XY/Kawamura coupling, uniform proposal width */
     const float *sigma_t;           /* XY: Gaussian width per temperature slot (NULL = uniform delta) */
     float coefficients[5], K, g_d, rho, mass; /* He3 */

@@ -66,3 +66,35 @@ def test_argument_validation_without_a_gpu(lib):
     assert lib.mc_create(0, ctypes.byref(params), Ls, 0, temps, 1, None, ctypes.byref(h)) == _lib.EINVAL
     assert lib.mc_get_error(None) == _lib.EINVAL and lib.mc_destroy(None) == 0
     assert lib.mc_sweep(None, 1) == _lib.EINVAL
+
+
+def test_window_sweep_limits_without_a_gpu(lib):
+    """A window of more than 2^24 sweeps, a sample interval above 2^24 and a
+    resident launch of more than 2^28 sweeps are refused on the host before
+    any CUDA call (the kernels count down to the next sample in an int)."""
+    import numpy as np
+
+    from mcgb import _lib
+    from mcgb.batch import REPLICA_DTYPE, BatchPT, BatchWindow
+    table = np.array([(16, 0, 0, 1, 0)], dtype=REPLICA_DTYPE)
+    w = BatchWindow()
+    # Device pointers are never dereferenced: the checks run first.
+    for name in ("table", "work_ptr", "work_idx", "state", "rng", "aux", "betas", "w2t", "e_run", "energies",
+                 "accepted", "clock"):
+        setattr(w, name, 256)
+    w.host_table = table.ctypes.data
+    w.n_replicas = w.n_clusters = w.cluster_size = 1
+    w.threads, w.J = 64, 1.0
+    w.n_sweeps = (1 << 24) + 1
+    assert lib.mcgb_batch_window_run(0, ctypes.byref(w), None) == _lib.EINVAL
+    assert "n_sweeps must be in [0, 16777216]" in _lib.last_error()
+    w.n_sweeps = 10
+    w.samples, w.n_slots, w.n_temps_total, w.sample_interval = 256, 1, 1, (1 << 24) + 1
+    assert lib.mcgb_batch_window_run(0, ctypes.byref(w), None) == _lib.EINVAL
+    assert "bad sample buffer" in _lib.last_error()
+    w.samples, w.sample_interval = None, 0
+    w.n_sweeps = 1 << 23
+    pt = BatchPT()
+    sync = (ctypes.c_int32 * 8)()
+    assert lib.mcgb_batch_run_resident(0, ctypes.byref(w), ctypes.byref(pt), sync, 64, None) == _lib.EINVAL
+    assert "sweeps a launch" in _lib.last_error()
